@@ -1,0 +1,149 @@
+"""ctypes bindings of the C ABI (include/diaq_gb300.h) of libdiaq_gb300.so.
+
+This is how a non-pybind caller -- a test, another language's FFI -- reaches the library; the
+``diaq_gpu`` module is the other way in.  Every wrapper raises ``DiaqError`` on a non-zero status
+with the library's message.  The library must have been built (``python -m diaq_gb300.build``);
+there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libdiaq_gb300.so")
+
+C128, C64 = 0, 1
+_lib = None
+
+# name -> (restype, argtypes); mirrors include/diaq_gb300.h
+P, I64, I32, F64, INT = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int
+SIGNATURES = {
+    "diaq_last_error": (ctypes.c_char_p, []),
+    "diaq_version": (ctypes.c_char_p, []),
+    "diaq_matrix_create": (INT, [I64, I64, I32, P, P, P, INT, INT, P, P]),
+    "diaq_matrix_destroy": (INT, [P]),
+    "diaq_matrix_info": (INT, [P, P, P, P, P, P]),
+    "diaq_matrix_offsets": (INT, [P, P]),
+    "diaq_matrix_download": (INT, [P, P, P, INT, P]),
+    "diaq_matrix_copy": (INT, [P, P, P]),
+    "diaq_matrix_convert": (INT, [P, INT, P, P]),
+    "diaq_matrix_prune": (INT, [P, P, P]),
+    "diaq_spmv_z": (INT, [P, P, P, P, P, P]),
+    "diaq_spmv_c": (INT, [P, P, P, P, P, P]),
+    "diaq_spmm": (INT, [P, INT, P, P, I64, P, P, I64, P]),
+    "diaq_spmv_host": (INT, [P, P, P, P, P]),
+    "diaq_spmv_ntimes_host": (INT, [P, P, P, INT, P, P]),
+    "diaq_spgemm_symbolic": (INT, [P, P, P, P, P]),
+    "diaq_spgemm_numeric": (INT, [P, P, P, P]),
+    "diaq_spgemm": (INT, [P, P, INT, P, P]),
+    "diaq_norm1_est": (INT, [P, P, P]),
+    "diaq_frobenius": (INT, [P, P, P]),
+    "diaq_pow": (INT, [P, INT, INT, P, P]),
+    "diaq_expm_negative": (INT, [P, F64, INT, F64, F64, INT, P, P, P, P]),
+    "diaq_expm": (INT, [P, INT, F64, F64, INT, P, P]),
+    "diaq_ham_sim": (INT, [P, P, P, F64, I64, INT, P, P, P]),
+    "diaq_ham_sim_host": (INT, [P, P, P, F64, I64, INT, P, P]),
+    "diaq_select_sm": (INT, [F64, F64, F64, F64, INT, P, P]),
+}
+
+
+class DiaqError(RuntimeError):
+    pass
+
+
+def lib():
+    """Load libdiaq_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m diaq_gb300.build` (nvcc, sm_103a)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status != 0:
+        raise DiaqError(lib().diaq_last_error().decode())
+
+
+def ptr(a) -> int:
+    """Data pointer of a numpy array or a torch tensor (or an int)."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+def select_sm(norm1: float, tau: float, tol: float, scale_cutoff: float = 1.0, max_m: int = 100):
+    """(substeps_log2, m) of the norm-bound rule (diaq_select_sm)."""
+    s, m = ctypes.c_int(), ctypes.c_int()
+    check(lib().diaq_select_sm(norm1, tau, tol, scale_cutoff, max_m, ctypes.byref(s), ctypes.byref(m)))
+    return s.value, m.value
+
+
+class Matrix:
+    """Owning handle of a device matrix (diaq_matrix_t)."""
+
+    def __init__(self, handle):
+        self.h = ctypes.c_void_p(handle) if not isinstance(handle, ctypes.c_void_p) else handle
+
+    @staticmethod
+    def create(rows, cols, offsets, re=None, im=None, precision=C128, on_device=False, stream=None) -> "Matrix":
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        if re is not None and not on_device:
+            re = np.ascontiguousarray(re, dtype=np.float64)
+            im = np.ascontiguousarray(im, dtype=np.float64)
+        out = ctypes.c_void_p()
+        check(lib().diaq_matrix_create(rows, cols, len(off), off.ctypes.data, ptr(re), ptr(im),
+                                       1 if on_device else 0, precision, stream, ctypes.byref(out)))
+        return Matrix(out)
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.diaq_matrix_destroy(self.h)
+            self.h = None
+
+    def info(self):
+        r, c, t = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        nd, p = ctypes.c_int32(), ctypes.c_int()
+        check(lib().diaq_matrix_info(self.h, ctypes.byref(r), ctypes.byref(c), ctypes.byref(nd), ctypes.byref(t),
+                                     ctypes.byref(p)))
+        return r.value, c.value, nd.value, t.value, p.value
+
+    def offsets(self) -> np.ndarray:
+        nd = self.info()[2]
+        off = np.empty(max(nd, 1), dtype=np.int32)
+        check(lib().diaq_matrix_offsets(self.h, off.ctypes.data))
+        return off[:nd]
+
+    def download(self):
+        """(offsets, re, im) packed, float64, on the host."""
+        rows, cols, nd, total, _ = self.info()
+        re, im = np.empty(max(total, 1)), np.empty(max(total, 1))
+        check(lib().diaq_matrix_download(self.h, re.ctypes.data, im.ctypes.data, 0, None))
+        return self.offsets(), re[:total], im[:total]
+
+    def _new(self, fn, *args) -> "Matrix":
+        out = ctypes.c_void_p()
+        check(fn(self.h, *args, ctypes.byref(out)))
+        return Matrix(out)
+
+    def copy(self):
+        return self._new(lib().diaq_matrix_copy, None)
+
+    def convert(self, precision):
+        return self._new(lib().diaq_matrix_convert, precision, None)
+
+    def prune(self):
+        return self._new(lib().diaq_matrix_prune, None)

@@ -1,0 +1,516 @@
+// Norms, elementwise helpers, pow and the matrix exponential on device matrices.
+// Replaces estimate_1norm / norm / add / divide_by_int / copy_and_scale_by_imag
+// (src/diaQMatrix.hpp:867-1358), pow / pow_cuda (src/spPow.cpp:19-56, src/spPow_gpu.cu:21-56)
+// and expm(_negative)_taylor(_scaled)(_cuda) (src/spME.cpp:13-295, src/spME_gpu.cu:10-294).
+// The Taylor loop runs on the host over device-resident matrices: every term is one device
+// SpGEMM; nothing is copied back except the scalar norms that steer the loop.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+
+#include "spmv_kernel.cuh"
+
+namespace diaq_gb300 {
+
+int spgemm(const Matrix &A, const Matrix &B, bool prune, cudaStream_t s, Matrix **out);
+
+// ---- norms ---------------------------------------------------------------------------------------
+// Column sums of |re|+|im| (one thread per column, diagonals in slot order), max over columns via
+// an integer atomicMax on the bit pattern (valid for non-negative doubles).
+template <typename T>
+__global__ void colsum_max_kernel(const DiagMeta *__restrict__ meta, int nd, const T *__restrict__ re,
+                                  const T *__restrict__ im, int64_t cols, unsigned long long *__restrict__ out) {
+    __shared__ DiagMeta sm[kMetaChunk];
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double sum = 0.0;
+    for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
+        const int cn = min(kMetaChunk, nd - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cn; i += blockDim.x) sm[i] = meta[c0 + i];
+        __syncthreads();
+        if (c >= cols) continue;
+        for (int k = 0; k < cn; ++k) {
+            const int64_t r = c - sm[k].off;
+            if (r >= sm[k].lo && r < sm[k].hi)
+                sum += fabs((double)re[sm[k].base + r]) + fabs((double)im[sm[k].base + r]);
+        }
+    }
+    // block max, then one atomic per block
+    for (int o = 16; o > 0; o >>= 1) sum = fmax(sum, __shfl_down_sync(0xffffffffu, sum, o));
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+// Sum of squares over the whole value buffer (gaps hold zeros): per-block partials, fixed order.
+template <typename T>
+__global__ void sumsq_partial_kernel(const T *__restrict__ re, const T *__restrict__ im, int64_t n,
+                                     double *__restrict__ part) {
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double a = re[i], b = im[i];
+        s += a * a + b * b;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) part[blockIdx.x] = v;
+    }
+}
+
+__global__ void sum_partials_kernel(const double *__restrict__ part, int n, double *__restrict__ out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) *out = v;
+    }
+}
+
+int norm1_est(const Matrix &A, double *out, cudaStream_t s) {
+    *out = 0.0;
+    if (A.nd == 0 || A.cols == 0) return DIAQ_OK;
+    unsigned long long *d = nullptr;
+    DQ_CUDA(cudaMallocAsync(&d, sizeof(unsigned long long), s));
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) {
+        const unsigned grid = (unsigned)((A.cols + 255) / 256);
+        if (A.prec == DIAQ_C128)
+            colsum_max_kernel<double><<<grid, 256, 0, s>>>(A.d_meta, A.nd, (const double *)A.re, (const double *)A.im, A.cols, d);
+        else
+            colsum_max_kernel<float><<<grid, 256, 0, s>>>(A.d_meta, A.nd, (const float *)A.re, (const float *)A.im, A.cols, d);
+        e = cudaGetLastError();
+    }
+    unsigned long long bits = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, d, sizeof(bits), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(d, s);
+    if (e != cudaSuccess) return cuda_status(e, "norm1_est", __FILE__, __LINE__);
+    std::memcpy(out, &bits, sizeof(double));
+    return DIAQ_OK;
+}
+
+int frobenius(const Matrix &A, double *out, cudaStream_t s) {
+    *out = 0.0;
+    if (A.capacity == 0) return DIAQ_OK;
+    const int nblk = (int)std::min<int64_t>((A.capacity + 255) / 256, 2 * num_sms());
+    double *d = nullptr;
+    DQ_CUDA(cudaMallocAsync(&d, sizeof(double) * (nblk + 1), s));
+    if (A.prec == DIAQ_C128)
+        sumsq_partial_kernel<double><<<nblk, 256, 0, s>>>((const double *)A.re, (const double *)A.im, A.capacity, d + 1);
+    else
+        sumsq_partial_kernel<float><<<nblk, 256, 0, s>>>((const float *)A.re, (const float *)A.im, A.capacity, d + 1);
+    sum_partials_kernel<<<1, 256, 0, s>>>(d + 1, nblk, d);
+    cudaError_t e = cudaGetLastError();
+    double v = 0.0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&v, d, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(d, s);
+    if (e != cudaSuccess) return cuda_status(e, "frobenius", __FILE__, __LINE__);
+    *out = std::sqrt(v);
+    return DIAQ_OK;
+}
+
+// ---- elementwise ---------------------------------------------------------------------------------
+enum ScaleOp { kTimesI = 0, kDivInt = 1, kTimesReal = 2 };
+
+// In place over the whole buffer (gaps stay zero):
+//  kTimesI:    (re, im) <- (-1 * im * c, re * c), diaQMatrix::copy_and_scale_by_imag(c)
+//  kDivInt:    (re, im) <- (re / c, im / c),     diaQMatrix::divide_by_int(c)
+//  kTimesReal: (re, im) <- (re * c, im * c),     diaQMatrix::scale_by_real(c)
+template <typename T>
+__global__ void scale_kernel(T *__restrict__ re, T *__restrict__ im, int64_t n, int op, double c) {
+    const T cc = (T)c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T a = re[i], b = im[i];
+        if (op == kTimesI) {
+            re[i] = (T)-1.0 * b * cc;
+            im[i] = a * cc;
+        } else if (op == kDivInt) {
+            re[i] = a / cc;
+            im[i] = b / cc;
+        } else {
+            re[i] = a * cc;
+            im[i] = b * cc;
+        }
+    }
+}
+
+int scale(Matrix &A, int op, double c, cudaStream_t s) {
+    if (A.capacity == 0) return DIAQ_OK;
+    const int grid = (int)std::min<int64_t>((A.capacity + 255) / 256, 8 * num_sms());
+    if (A.prec == DIAQ_C128)
+        scale_kernel<double><<<grid, 256, 0, s>>>((double *)A.re, (double *)A.im, A.capacity, op, c);
+    else
+        scale_kernel<float><<<grid, 256, 0, s>>>((float *)A.re, (float *)A.im, A.capacity, op, c);
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
+}
+
+// C diagonal k = A[sa[k]] + sign * B[sb[k]] (either slot may be -1: absent).
+template <typename T>
+__global__ void union_add_kernel(const DiagMeta *__restrict__ mA, const T *__restrict__ Are, const T *__restrict__ Aim,
+                                 const DiagMeta *__restrict__ mB, const T *__restrict__ Bre, const T *__restrict__ Bim,
+                                 const DiagMeta *__restrict__ mC, T *__restrict__ Cre, T *__restrict__ Cim,
+                                 const int2 *__restrict__ slots, int nd, T sign) {
+    for (int k = blockIdx.y; k < nd; k += gridDim.y) {
+        const DiagMeta mc = mC[k];
+        const int2 sl = slots[k];
+        const int64_t ab = sl.x >= 0 ? mA[sl.x].base : 0, bb = sl.y >= 0 ? mB[sl.y].base : 0;
+        for (int64_t r = mc.lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < mc.hi;
+             r += (int64_t)gridDim.x * blockDim.x) {
+            if (sl.x >= 0 && sl.y >= 0) {
+                Cre[mc.base + r] = Are[ab + r] + sign * Bre[bb + r];
+                Cim[mc.base + r] = Aim[ab + r] + sign * Bim[bb + r];
+            } else if (sl.x >= 0) {
+                Cre[mc.base + r] = Are[ab + r];
+                Cim[mc.base + r] = Aim[ab + r];
+            } else {
+                Cre[mc.base + r] = sign * Bre[bb + r];
+                Cim[mc.base + r] = sign * Bim[bb + r];
+            }
+        }
+    }
+}
+
+// A + sign * B over the union of the offsets, ascending (diaQMatrix::combined,
+// src/diaQMatrix.hpp:867-916).
+int union_add(const Matrix &A, const Matrix &B, double sign, cudaStream_t s, Matrix **out) {
+    if (A.rows != B.rows || A.cols != B.cols) return set_error(DIAQ_ERR_INVALID, "diaQMatrix::add: shape mismatch");
+    std::map<int32_t, int2> u;
+    for (int32_t k = 0; k < A.nd; ++k) u[A.off[k]] = make_int2(k, -1);
+    for (int32_t k = 0; k < B.nd; ++k) {
+        auto it = u.find(B.off[k]);
+        if (it == u.end()) u[B.off[k]] = make_int2(-1, k);
+        else it->second.y = k;
+    }
+    std::vector<int32_t> off;
+    std::vector<int2> slots;
+    for (auto &kv : u) {
+        off.push_back(kv.first);
+        slots.push_back(kv.second);
+    }
+    Matrix *C = nullptr;
+    DQ_TRY(make_zero(A.rows, A.cols, (int32_t)off.size(), off.data(), A.prec, s, &C));
+    if (C->nd == 0) {
+        *out = C;
+        return DIAQ_OK;
+    }
+    int2 *d = nullptr;
+    cudaError_t e = cudaMallocAsync(&d, sizeof(int2) * slots.size(), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, slots.data(), sizeof(int2) * slots.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        int64_t maxlen = 1;
+        for (const auto &m : C->meta) maxlen = std::max(maxlen, m.hi - m.lo);
+        const dim3 g((unsigned)std::min<int64_t>((maxlen + 255) / 256, 4 * num_sms()),
+                     (unsigned)std::min<int64_t>(C->nd, 65535));
+        if (A.prec == DIAQ_C128)
+            union_add_kernel<double><<<g, 256, 0, s>>>(A.d_meta, (const double *)A.re, (const double *)A.im, B.d_meta,
+                                                       (const double *)B.re, (const double *)B.im, C->d_meta,
+                                                       (double *)C->re, (double *)C->im, d, C->nd, sign);
+        else
+            union_add_kernel<float><<<g, 256, 0, s>>>(A.d_meta, (const float *)A.re, (const float *)A.im, B.d_meta,
+                                                      (const float *)B.re, (const float *)B.im, C->d_meta,
+                                                      (float *)C->re, (float *)C->im, d, C->nd, (float)sign);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // slots (host) must outlive the copy
+    if (d) cudaFreeAsync(d, s);
+    if (e != cudaSuccess) {
+        destroy(C);
+        return cuda_status(e, "union add", __FILE__, __LINE__);
+    }
+    *out = C;
+    return DIAQ_OK;
+}
+
+template <typename T>
+__global__ void fill_diag_kernel(T *__restrict__ re, T *__restrict__ im, int64_t base, int64_t lo, int64_t hi, T vr,
+                                 T vi) {
+    for (int64_t r = lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < hi; r += (int64_t)gridDim.x * blockDim.x) {
+        re[base + r] = vr;
+        im[base + r] = vi;
+    }
+}
+
+// identityMatrix(n) (src/specialMatrices.hpp:9-24).
+int identity(int64_t n, int prec, cudaStream_t s, Matrix **out) {
+    const int32_t zero = 0;
+    Matrix *I = nullptr;
+    DQ_TRY(make_zero(n, n, n > 0 ? 1 : 0, &zero, prec, s, &I));
+    if (n > 0) {
+        const DiagMeta &m = I->meta[0];
+        const int grid = (int)std::min<int64_t>((n + 255) / 256, 4 * num_sms());
+        if (prec == DIAQ_C128)
+            fill_diag_kernel<double><<<grid, 256, 0, s>>>((double *)I->re, (double *)I->im, m.base, m.lo, m.hi, 1.0, 0.0);
+        else
+            fill_diag_kernel<float><<<grid, 256, 0, s>>>((float *)I->re, (float *)I->im, m.base, m.lo, m.hi, 1.f, 0.f);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            destroy(I);
+            return cuda_status(e, "identity", __FILE__, __LINE__);
+        }
+    }
+    *out = I;
+    return DIAQ_OK;
+}
+
+// Single-diagonal fast path of the Taylor routines (src/spME.cpp:96-118 and :172-198): the
+// result is the identity with its main diagonal's first len(A's diagonal) values replaced by
+//   negative = 0:  exp(a) (cos b, sin b)              (expm_taylor)
+//   negative = 1:  exp(t b) (cos(t a), -sin(t a))     (expm_negative_taylor)
+// where a + ib runs over A's only diagonal -- the main one in the intended use; the reference
+// applies the same rule whatever the diagonal's offset, and so does this.
+template <typename T>
+__global__ void single_diag_exp_kernel(const T *__restrict__ are, const T *__restrict__ aim, int64_t abase,
+                                       T *__restrict__ re, T *__restrict__ im, int64_t base, int64_t len, int negative,
+                                       double t) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+        const double a = are[abase + i], b = aim[abase + i];
+        if (negative) {
+            const double ta = t * a, tb = t * b;
+            const double eb = exp(tb);
+            re[base + i] = (T)(eb * cos(ta));
+            im[base + i] = (T)(-eb * sin(ta));
+        } else {
+            const double ea = exp(a);
+            re[base + i] = (T)(ea * cos(b));
+            im[base + i] = (T)(ea * sin(b));
+        }
+    }
+}
+
+int single_diag_exp(const Matrix &A, int negative, double t, cudaStream_t s, Matrix **out) {
+    Matrix *R = nullptr;
+    DQ_TRY(identity(A.rows, A.prec, s, &R));
+    const DiagMeta &ma = A.meta[0];
+    const int64_t len = ma.hi - ma.lo;
+    const DiagMeta &mr = R->meta[0];
+    if (len > 0) {
+        const int grid = (int)std::min<int64_t>((len + 255) / 256, 4 * num_sms());
+        if (A.prec == DIAQ_C128)
+            single_diag_exp_kernel<double><<<grid, 256, 0, s>>>((const double *)A.re, (const double *)A.im, ma.base + ma.lo,
+                                                                (double *)R->re, (double *)R->im, mr.base + mr.lo, len,
+                                                                negative, t);
+        else
+            single_diag_exp_kernel<float><<<grid, 256, 0, s>>>((const float *)A.re, (const float *)A.im, ma.base + ma.lo,
+                                                               (float *)R->re, (float *)R->im, mr.base + mr.lo, len,
+                                                               negative, t);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            destroy(R);
+            return cuda_status(e, "single-diagonal exp", __FILE__, __LINE__);
+        }
+    }
+    *out = R;
+    return DIAQ_OK;
+}
+
+// ---- pow ------------------------------------------------------------------------------------------
+int pow_matrix(const Matrix &A, int n, bool prune, cudaStream_t s, Matrix **out) {
+    if (n < 0) return set_error(DIAQ_ERR_INVALID, "pow: negative exponent not supported");
+    if (A.rows != A.cols) return set_error(DIAQ_ERR_INVALID, "pow: matrix must be square");
+    if (n == 0) return identity(A.rows, A.prec, s, out);
+    Matrix *base = nullptr;
+    DQ_TRY(copy_as(A, A.prec, s, &base));
+    if (n == 1) {
+        *out = base;
+        return DIAQ_OK;
+    }
+    const uint64_t e0 = (uint64_t)n;
+    if ((e0 & (e0 - 1)) == 0) {  // 2^s: s squarings
+        for (uint64_t e = e0; e > 1; e >>= 1) {
+            Matrix *sq = nullptr;
+            const int st = spgemm(*base, *base, prune, s, &sq);
+            destroy(base);
+            if (st != DIAQ_OK) return st;
+            base = sq;
+        }
+        *out = base;
+        return DIAQ_OK;
+    }
+    // binary exponentiation; result starts at the first odd power (src/spPow_gpu.cu:43-53)
+    Matrix *result = nullptr;
+    uint64_t e = e0;
+    int st = DIAQ_OK;
+    while (e > 0 && st == DIAQ_OK) {
+        if (e & 1ULL) {
+            Matrix *r2 = nullptr;
+            if (result) {
+                st = spgemm(*result, *base, prune, s, &r2);
+                destroy(result);
+            } else {
+                st = copy_as(*base, base->prec, s, &r2);
+            }
+            result = r2;
+        }
+        e >>= 1ULL;
+        if (e && st == DIAQ_OK) {
+            Matrix *b2 = nullptr;
+            st = spgemm(*base, *base, prune, s, &b2);
+            destroy(base);
+            base = b2;
+        }
+    }
+    destroy(base);
+    if (st != DIAQ_OK) {
+        destroy(result);
+        return st;
+    }
+    *out = result;
+    return DIAQ_OK;
+}
+
+// ---- exponential -----------------------------------------------------------------------------------
+static int scaling_exponent(double norm, double t_abs, double cutoff) {
+    const double scaled = t_abs * norm + 1e-12;  // src/spME.cpp:256-262
+    return scaled > cutoff ? (int)std::ceil(std::log2(scaled / cutoff)) : 0;
+}
+
+// Taylor series of exp(X) with X prepared by the caller; term_k = term_{k-1} X / k.
+static int taylor(const Matrix &X, int max_it, double tol, bool prune, cudaStream_t s, Matrix **out, int *terms) {
+    Matrix *result = nullptr, *term = nullptr;
+    DQ_TRY(identity(X.rows, X.prec, s, &result));
+    int st = identity(X.rows, X.prec, s, &term);
+    int k = 0;
+    for (k = 1; k <= max_it && st == DIAQ_OK; ++k) {
+        Matrix *t2 = nullptr;
+        st = spgemm(*term, X, prune, s, &t2);
+        destroy(term);
+        term = t2;
+        if (st != DIAQ_OK) break;
+        st = scale(*term, kDivInt, (double)k, s);
+        if (st != DIAQ_OK) break;
+        Matrix *r2 = nullptr;
+        st = union_add(*result, *term, 1.0, s, &r2);
+        if (st != DIAQ_OK) break;
+        destroy(result);
+        result = r2;
+        double nrm = 0.0;
+        st = frobenius(*term, &nrm, s);
+        if (st != DIAQ_OK) break;
+        if (nrm < tol) break;
+    }
+    destroy(term);
+    if (st != DIAQ_OK) {
+        destroy(result);
+        return st;
+    }
+    if (terms) *terms = std::min(k, max_it);
+    *out = result;
+    return DIAQ_OK;
+}
+
+int expm_negative(const Matrix &A, double t, int max_it, double cutoff, double tol, bool prune, cudaStream_t s,
+                  Matrix **out, int *s_out, int *terms_out) {
+    if (A.rows != A.cols) return set_error(DIAQ_ERR_INVALID, "expm_negative: matrix must be square");
+    if (s_out) *s_out = 0;
+    if (terms_out) *terms_out = 0;
+    if (A.nd == 1) return single_diag_exp(A, 1, t, s, out);
+    double nrm = 0.0;
+    DQ_TRY(norm1_est(A, &nrm, s));
+    const int sc = scaling_exponent(nrm, std::fabs(t), cutoff);
+    const double ts = std::ldexp(t, -sc);
+    const double tol_s = std::max(1e-15, tol * std::ldexp(1.0, -sc));
+    Matrix *X = nullptr;
+    DQ_TRY(copy_as(A, A.prec, s, &X));
+    int st = scale(*X, kTimesI, -ts, s);  // X = -i t_s A
+    Matrix *U = nullptr;
+    int terms = 0;
+    if (st == DIAQ_OK) st = taylor(*X, max_it, tol_s, prune, s, &U, &terms);
+    destroy(X);
+    if (st != DIAQ_OK) return st;
+    Matrix *P = nullptr;
+    st = pow_matrix(*U, 1 << sc, prune, s, &P);
+    destroy(U);
+    if (st != DIAQ_OK) return st;
+    if (s_out) *s_out = sc;
+    if (terms_out) *terms_out = terms;
+    *out = P;
+    return DIAQ_OK;
+}
+
+int expm(const Matrix &A, int max_it, double cutoff, double tol, bool prune, cudaStream_t s, Matrix **out) {
+    if (A.rows != A.cols) return set_error(DIAQ_ERR_INVALID, "expm: matrix must be square");
+    if (A.nd == 1) return single_diag_exp(A, 0, 0.0, s, out);
+    double nrm = 0.0;
+    DQ_TRY(norm1_est(A, &nrm, s));
+    const int sc = scaling_exponent(nrm, 1.0, cutoff);
+    const double inv = std::ldexp(1.0, -sc);
+    const double tol_s = std::max(1e-15, tol * inv);
+    Matrix *X = nullptr;
+    DQ_TRY(copy_as(A, A.prec, s, &X));
+    int st = scale(*X, kTimesReal, inv, s);
+    Matrix *U = nullptr;
+    if (st == DIAQ_OK) st = taylor(*X, max_it, tol_s, prune, s, &U, nullptr);
+    destroy(X);
+    if (st != DIAQ_OK) return st;
+    Matrix *P = nullptr;
+    st = pow_matrix(*U, 1 << sc, prune, s, &P);
+    destroy(U);
+    if (st != DIAQ_OK) return st;
+    *out = P;
+    return DIAQ_OK;
+}
+
+}  // namespace diaq_gb300
+
+using namespace diaq_gb300;
+
+extern "C" {
+
+int diaq_norm1_est(diaq_matrix_t A, double *out, void *stream) {
+    if (!A || !out) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    return norm1_est(*A, out, (cudaStream_t)stream);
+}
+
+int diaq_frobenius(diaq_matrix_t A, double *out, void *stream) {
+    if (!A || !out) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    return frobenius(*A, out, (cudaStream_t)stream);
+}
+
+int diaq_pow(diaq_matrix_t A, int n, int prune, void *stream, diaq_matrix_t *out) {
+    if (!A || !out) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    Matrix *M = nullptr;
+    DQ_TRY(pow_matrix(*A, n, prune != 0, (cudaStream_t)stream, &M));
+    *out = handle(M);
+    return DIAQ_OK;
+}
+
+int diaq_expm_negative(diaq_matrix_t A, double t, int max_iterations, double scale_cutoff,
+                       double tolerance, int prune, void *stream, diaq_matrix_t *U, int *s_out,
+                       int *terms_out) {
+    if (!A || !U) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    Matrix *M = nullptr;
+    DQ_TRY(expm_negative(*A, t, max_iterations, scale_cutoff, tolerance, prune != 0, (cudaStream_t)stream, &M, s_out,
+                         terms_out));
+    *U = handle(M);
+    return DIAQ_OK;
+}
+
+int diaq_expm(diaq_matrix_t A, int max_iterations, double scale_cutoff, double tolerance, int prune,
+              void *stream, diaq_matrix_t *U) {
+    if (!A || !U) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    Matrix *M = nullptr;
+    DQ_TRY(expm(*A, max_iterations, scale_cutoff, tolerance, prune != 0, (cudaStream_t)stream, &M));
+    *U = handle(M);
+    return DIAQ_OK;
+}
+
+}  // extern "C"

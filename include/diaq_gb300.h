@@ -1,0 +1,194 @@
+/*
+ * diaq_gb300.h -- C ABI of libdiaq_gb300.so, the GB300 (sm_103a) implementation of DiaQ's
+ * diagonal-sparse hot path: complex SpMV, diagonal-pair SpGEMM with its structural dry-run,
+ * Taylor + scaling-and-squaring matrix exponential, and Hamiltonian time evolution.
+ *
+ * Conventions
+ *  - Every function returns a diaq_status (0 = DIAQ_OK).  On failure diaq_last_error() gives a
+ *    message for the calling thread.  CUDA failures read "CUDA error: <text> (file:line)", the
+ *    text the reference raises (src/cuda_check.hpp:11-18).
+ *  - A matrix is the DiaQ format: rows x cols, ndiag distinct diagonal offsets in slot order
+ *    (column = row + offset), and the values of each diagonal back to back in two float64
+ *    arrays re[] / im[] ("packed": diagonal k starts at sum of the lengths of diagonals < k;
+ *    the length of diagonal d is min(rows, cols) minus the part outside the matrix), the device
+ *    layout of the reference (src/deviceMatrix_gpu.cu:30-55).
+ *  - Vectors are SoA: separate real and imaginary arrays.  Several right-hand sides are stored
+ *    one after another with leading dimension ld (element (q, i) at x[q * ld + i]).
+ *  - `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).  Functions
+ *    documented as asynchronous only enqueue work; the others return after the work is done.
+ *  - Sizes are 64-bit; diagonal offsets are int32.
+ */
+#ifndef DIAQ_GB300_H
+#define DIAQ_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    DIAQ_OK = 0,
+    DIAQ_ERR_INVALID = 1,     /* bad argument: shapes, offsets, null pointers */
+    DIAQ_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    DIAQ_ERR_OOM = 3,         /* device allocation failed */
+    DIAQ_ERR_UNSUPPORTED = 4, /* valid request this build does not handle */
+    DIAQ_ERR_TIMEOUT = 5      /* a bounded device-side wait gave up */
+} diaq_status;
+
+typedef enum {
+    DIAQ_C128 = 0, /* complex double, SoA float64 */
+    DIAQ_C64 = 1   /* complex float, SoA float32 */
+} diaq_precision;
+
+typedef struct diaq_matrix_s *diaq_matrix_t;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *diaq_last_error(void);
+
+/* Library version string. */
+const char *diaq_version(void);
+
+/* ------------------------------------------------------------------------------------------
+ * Device matrices.  Replace deviceDiaQMatrix (src/deviceMatrix_gpu.hpp:37-68,
+ * src/deviceMatrix_gpu.cu:30-113).
+ * ---------------------------------------------------------------------------------------- */
+
+/* Create a device matrix from packed float64 values (re/im on the host, or on the device when
+ * values_on_device != 0).  precision DIAQ_C64 rounds the values to float32 on the device.
+ * re/im may both be NULL for a matrix of zeros.  Offsets must be distinct and inside the
+ * matrix.  Replaces deviceDiaQMatrix(const shared_ptr<diaQMatrix>&) (src/deviceMatrix_gpu.cu:58-76). */
+int diaq_matrix_create(int64_t rows, int64_t cols, int32_t ndiag, const int32_t *offsets,
+                       const double *re, const double *im, int values_on_device, int precision,
+                       void *stream, diaq_matrix_t *out);
+
+/* Free a device matrix (NULL is ignored).  Replaces ~deviceDiaQMatrix (src/deviceMatrix_gpu.cu:78-85). */
+int diaq_matrix_destroy(diaq_matrix_t A);
+
+/* Shape, diagonal count, stored (packed) value count and precision. */
+int diaq_matrix_info(diaq_matrix_t A, int64_t *rows, int64_t *cols, int32_t *ndiag,
+                     int64_t *total, int *precision);
+
+/* Copy the offsets (slot order) to a host array of ndiag entries. */
+int diaq_matrix_offsets(diaq_matrix_t A, int32_t *offsets);
+
+/* Packed float64 values to re/im (host arrays, or device arrays when dst_on_device != 0).
+ * Replaces deviceDiaQMatrix::to_host (src/deviceMatrix_gpu.cu:97-113). */
+int diaq_matrix_download(diaq_matrix_t A, double *re, double *im, int dst_on_device, void *stream);
+
+/* A second device matrix with the same values.  Replaces deviceDiaQMatrix::copy
+ * (src/deviceMatrix_gpu.cu:87-95). */
+int diaq_matrix_copy(diaq_matrix_t A, void *stream, diaq_matrix_t *out);
+
+/* The same matrix in another precision (c128 -> c64 rounds to nearest). */
+int diaq_matrix_convert(diaq_matrix_t A, int precision, void *stream, diaq_matrix_t *out);
+
+/* Drop the diagonals whose values are all exactly zero (real and imaginary == 0.0).  Replaces
+ * diaQMatrix::pruneMatrix (src/diaQMatrix.hpp:1543-1604). */
+int diaq_matrix_prune(diaq_matrix_t A, void *stream, diaq_matrix_t *out);
+
+/* ------------------------------------------------------------------------------------------
+ * SpMV.  Replaces spmv_device (src/spMV_gpu.cu:142-168): y = A x on device arrays, y
+ * overwritten, asynchronous on stream.
+ * ---------------------------------------------------------------------------------------- */
+
+/* c128 matrix, float64 vectors. */
+int diaq_spmv_z(diaq_matrix_t A, const double *x_re, const double *x_im, double *y_re,
+                double *y_im, void *stream);
+
+/* c64 matrix, float32 vectors. */
+int diaq_spmv_c(diaq_matrix_t A, const float *x_re, const float *x_im, float *y_re, float *y_im,
+                void *stream);
+
+/* nrhs right-hand sides at once (each diagonal value is read once per launch); vectors of the
+ * matrix's precision, element (q, i) at x[q*ldx + i], y[q*ldy + i]. */
+int diaq_spmm(diaq_matrix_t A, int nrhs, const void *x_re, const void *x_im, int64_t ldx,
+              void *y_re, void *y_im, int64_t ldy, void *stream);
+
+/* Host vectors in and out (x, y copied; A stays on the device).  Replaces
+ * spmv_cuda(shared_ptr<deviceDiaQMatrix>, x) (src/spMV_gpu.cu:170-204).  c128 only.  Synchronous. */
+int diaq_spmv_host(diaq_matrix_t A, const double *x_re, const double *x_im, double *y_re,
+                   double *y_im);
+
+/* y = A^n x by n repeated products on the device, host vectors.  n = 0 copies x (square A
+ * only); n > 1 needs a square A.  Replaces spMV_ntimes_cuda (src/spMV_ntimes_gpu.cu:61-263).
+ * c128 only.  Synchronous. */
+int diaq_spmv_ntimes_host(diaq_matrix_t A, const double *x_re, const double *x_im, int n,
+                          double *y_re, double *y_im);
+
+/* ------------------------------------------------------------------------------------------
+ * SpGEMM.  Replaces product_device / product_cuda (src/spGEMM_gpu.cu:84-161) and the host
+ * dry-run of product (src/spGEMM.cpp:346-378).
+ * ---------------------------------------------------------------------------------------- */
+
+/* Structural dry-run on the device: the ascending distinct offsets dA+dB inside
+ * [-(rowsA-1), colsB-1].  offsets_out (host) needs room for ndiagA*ndiagB entries; *count
+ * receives the number written.  Synchronous. */
+int diaq_spgemm_symbolic(diaq_matrix_t A, diaq_matrix_t B, int32_t *offsets_out, int32_t *count,
+                         void *stream);
+
+/* Numeric pass into C, whose offsets must come from diaq_spgemm_symbolic(A, B) (every product
+ * diagonal present); per result diagonal the pairs are summed in A-slot order.  Asynchronous. */
+int diaq_spgemm_numeric(diaq_matrix_t A, diaq_matrix_t B, diaq_matrix_t C, void *stream);
+
+/* C = A B (dry-run + numeric); prune != 0 also drops exact-zero diagonals, as the host entry
+ * point `product` does (src/spGEMM.cpp:516-534); product(DeviceMatrix, DeviceMatrix) does not.
+ * A and B must have the same precision.  Synchronous. */
+int diaq_spgemm(diaq_matrix_t A, diaq_matrix_t B, int prune, void *stream, diaq_matrix_t *C);
+
+/* ------------------------------------------------------------------------------------------
+ * Norms and the matrix exponential.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Max column sum of |re|+|im| (src/diaQMatrix.hpp:1287-1358).  Synchronous. */
+int diaq_norm1_est(diaq_matrix_t A, double *out, void *stream);
+
+/* Frobenius norm of the stored values (src/diaQMatrix.hpp:1255-1284).  Synchronous. */
+int diaq_frobenius(diaq_matrix_t A, double *out, void *stream);
+
+/* A^n: s squarings for n = 2^s, else binary exponentiation (src/spPow.cpp:19-56,
+ * src/spPow_gpu.cu:21-56).  prune as in diaq_spgemm. */
+int diaq_pow(diaq_matrix_t A, int n, int prune, void *stream, diaq_matrix_t *out);
+
+/* exp(-i t A) by Taylor + scaling and squaring: s = ceil(log2((|t| ||A||_1 + 1e-12)/cutoff)),
+ * Taylor terms of t/2^s until the Frobenius norm of a term < max(1e-15, tol 2^-s) or
+ * max_iterations, then s squarings (src/spME.cpp:230-295 with :158-223; its GPU twin
+ * src/spME_gpu.cu:156-294).  prune != 0 prunes every product as the CPU path does.
+ * s_out / terms_out may be NULL.  Synchronous. */
+int diaq_expm_negative(diaq_matrix_t A, double t, int max_iterations, double scale_cutoff,
+                       double tolerance, int prune, void *stream, diaq_matrix_t *U, int *s_out,
+                       int *terms_out);
+
+/* exp(A), same method (src/spME.cpp:13-150, src/spME_gpu.cu:10-150). */
+int diaq_expm(diaq_matrix_t A, int max_iterations, double scale_cutoff, double tolerance,
+              int prune, void *stream, diaq_matrix_t *U);
+
+/* ------------------------------------------------------------------------------------------
+ * Time evolution psi(t) = exp(-i H t) psi0.
+ * ---------------------------------------------------------------------------------------- */
+
+/* The reference's fused Hamiltonian simulation (hamiltonian_simulation_cuda,
+ * src/spHamSim_gpu_all_fused.cu:287-376): t is the TOTAL time, r steps of dt = t/r, each step
+ * exactly max_iterations Taylor terms (no scaling, no truncation test, no renormalisation);
+ * r = 0 copies psi0.  H must be square and c128; psi0 and psi_out are float64 device arrays of
+ * length N (psi_out may equal psi0).  Asynchronous. */
+int diaq_ham_sim(diaq_matrix_t H, const double *psi0_re, const double *psi0_im, double t,
+                 int64_t r, int max_iterations, double *psi_re, double *psi_im, void *stream);
+
+/* Norm-bound choice of the sub-step count and Taylor degree for one time step tau: the
+ * reference's scaling rule s = ceil(log2(tau*norm1/cutoff)) (src/spME.cpp:256-262) gives 2^s
+ * sub-steps of theta = tau*norm1/2^s each, and m is the smallest degree whose Taylor remainder
+ * bound theta^(m+1)/(m+1)! * exp(theta) is <= tol / 2^s (capped at max_m).  Host-only. */
+int diaq_select_sm(double norm1, double tau, double tol, double scale_cutoff, int max_m,
+                   int *substeps_log2, int *m);
+
+/* diaq_ham_sim with host vectors (psi0 uploaded once, the result downloaded once), as
+ * hamiltonian_simulation_cuda does.  Synchronous. */
+int diaq_ham_sim_host(diaq_matrix_t H, const double *psi0_re, const double *psi0_im, double t,
+                      int64_t r, int max_iterations, double *psi_re, double *psi_im);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIAQ_GB300_H */
