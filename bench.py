@@ -183,109 +183,190 @@ def cpu_baseline_sample(N, off, re, im, s, m):
             "sample": f"{steps} time step(s) of one state ({1 << s}x{m} SpMVs each) on the host, C/OpenMP"}
 
 
+def _timed(stream, fn):
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def _max_over_ranks(ms, world, dev):
+    import torch
+
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def _barrier(world):
+    import torch
+
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+
+def run_spmv_only(args):
+    """Repeated SpMV on the workload (c128 and c64), for profiling the kernel on its own."""
+    import torch
+
+    from diaq_gb300 import build, capi
+    from diaq_gb300 import hamiltonians as ham
+
+    build.build()
+    L = capi.lib()
+    N, off, re, im = workload(args.n)
+    H = capi.Matrix.create(N, N, off, re, im)
+    Hc = H.convert(capi.C64)
+    psi = ham.random_state(N, 0)
+    sp = torch.cuda.current_stream().cuda_stream
+    out = {}
+    for name, M, dt, fn in (("c128", H, torch.float64, L.diaq_spmv_z), ("c64", Hc, torch.float32, L.diaq_spmv_c)):
+        xr = torch.from_numpy(psi.real.copy()).to("cuda", dt)
+        xi = torch.from_numpy(psi.imag.copy()).to("cuda", dt)
+        yr, yi = torch.empty_like(xr), torch.empty_like(xi)
+        for _ in range(args.warmup):
+            capi.check(fn(M.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
+
+        def loop():
+            for i in range(args.spmv_reps):
+                a, b, c, d = (xr, xi, yr, yi) if i % 2 == 0 else (yr, yi, xr, xi)
+                capi.check(fn(M.h, a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), sp))
+
+        torch.cuda.synchronize()
+        us = 1e3 * _timed(torch.cuda.current_stream(), loop) / args.spmv_reps
+        w = 16 if name == "c128" else 8
+        by = w * int(re.size) + 2 * w * N
+        out[name] = {"us": us, "gbs": by / us / 1e3, "bytes": by}
+    print(json.dumps({"mode": "spmv", "n_qubits": args.n, **out}), flush=True)
+
+
 def run_ours(args, rank, world):
     import torch
 
     from diaq_gb300 import build, capi
+    from diaq_gb300 import hamiltonians as ham
 
     build.build()
     L = capi.lib()
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
     N, off, re, im = workload(args.n)
     total = int(re.size)
     H = capi.Matrix.create(N, N, off, re, im)
     norm1 = ctypes.c_double()
     capi.check(L.diaq_norm1_est(H.h, ctypes.byref(norm1), None))
-    s, m = plain_schedule(capi, norm1.value)
-    sub = 1 << s
-    from diaq_gb300 import hamiltonians as ham
+    K, W, S = args.steps, args.warmup, args.states
 
-    psi = ham.random_state(N, 0)
-    pr = torch.from_numpy(psi.real.copy()).to(dev)
-    pi = torch.from_numpy(psi.imag.copy()).to(dev)
-    stream = torch.cuda.current_stream(dev)
-    sp = stream.cuda_stream
+    # ---- plain c128 form: one state, the reference's scaling rule, remainder-bound m ----
+    s_p, m_p = capi.select_sm(norm1.value, DT, TOL_STEP, 1.0, 100)
+    plain = capi.Evolve(H, 1, capi.EVOLVE_C128)
+    p0 = ham.random_state(N, 0)
+    ppr = torch.from_numpy(p0.real.copy()).to(dev)
+    ppi = torch.from_numpy(p0.imag.copy()).to(dev)
+    plain.run(ppr, ppi, N, DT, W, s_p, m_p, sp)
+    _barrier(world)
+    ms_plain = _max_over_ranks(_timed(stream, lambda: plain.run(ppr, ppi, N, DT, K, s_p, m_p, sp)), world, dev)
+    lps_plain = plain.launches_per_step()
 
-    def evolve(k_steps):
-        capi.check(L.diaq_ham_sim(H.h, pr.data_ptr(), pi.data_ptr(), DT * k_steps, k_steps * sub, m,
-                                  pr.data_ptr(), pi.data_ptr(), sp))
-
-    # warm-up
-    evolve(args.warmup)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # ---- chosen form: S states per launch, complex64 terms + FP64 state, cost-optimal (s, m) ----
+    s_c, m_c = capi.select_sm_min_cost(norm1.value, DT, TOL_STEP, 12, 60)
+    chosen = capi.Evolve(H, S, capi.EVOLVE_MIXED)
+    P0 = ham.random_state(N, 0, k=S) if S > 1 else p0[None, :]
+    cpr = torch.from_numpy(np.ascontiguousarray(P0.real)).to(dev)
+    cpi = torch.from_numpy(np.ascontiguousarray(P0.imag)).to(dev)
+    chosen.run(cpr, cpi, N, DT, W, s_c, m_c, sp)
+    _barrier(world)
     with ClockSampler(dev.index) as clk:
-        e0.record(stream)
-        evolve(args.steps)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
-    launches = args.steps * sub * m
-    norm_drift = abs(float(torch.sqrt((pr * pr + pi * pi).sum()).item()) - 1.0)
+        ms = _max_over_ranks(_timed(stream, lambda: chosen.run(cpr, cpi, N, DT, K, s_c, m_c, sp)), world, dev)
+    lps = chosen.launches_per_step()
+    launches = K * lps + 2
 
-    # plain SpMV (1000 repeated products of config 2, the kernel's own roofline)
-    xr, xi = pr.clone(), pi.clone()
-    yr, yi = torch.empty_like(xr), torch.empty_like(xi)
-    reps = args.spmv_reps
-    for _ in range(5):
-        capi.check(L.diaq_spmv_z(H.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
+    # ---- accuracy of the chosen form: the same W + K steps in c128 at a tight tolerance ----
+    s_r, m_r = capi.select_sm(norm1.value, DT, 1e-14, 1.0, 100)
+    refp = capi.Evolve(H, S, capi.EVOLVE_C128)
+    rpr = torch.from_numpy(np.ascontiguousarray(P0.real)).to(dev)
+    rpi = torch.from_numpy(np.ascontiguousarray(P0.imag)).to(dev)
+    refp.run(rpr, rpi, N, DT, W + K, s_r, m_r, sp)
     torch.cuda.synchronize()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    for i in range(reps):
-        a, b = (xr, xi) if i % 2 == 0 else (yr, yi)
-        c, d = (yr, yi) if i % 2 == 0 else (xr, xi)
-        capi.check(L.diaq_spmv_z(H.h, a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), sp))
-    f1.record(stream)
-    torch.cuda.synchronize()
-    spmv_us = 1e3 * f0.elapsed_time(f1) / reps
+    got = (cpr.double() + 1j * cpi.double())
+    want = (rpr + 1j * rpi)
+    errs = (torch.linalg.vector_norm(got - want, dim=1) / torch.linalg.vector_norm(want, dim=1)).cpu().numpy()
+    fid = (torch.abs((want.conj() * got).sum(dim=1)) ** 2 /
+           (torch.linalg.vector_norm(got, dim=1) ** 2 * torch.linalg.vector_norm(want, dim=1) ** 2)).cpu().numpy()
+    del refp, rpr, rpi
 
-    # end to end through the C ABI with host buffers: psi0 up, K steps, psi down
-    hpr, hpi = np.ascontiguousarray(psi.real), np.ascontiguousarray(psi.imag)
-    opr, opi = np.empty(N), np.empty(N)
+    # ---- end to end through the C ABI with host buffers: S states up, K steps, S states down ----
+    hr = np.ascontiguousarray(P0.real).ravel().copy()
+    hi = np.ascontiguousarray(P0.imag).ravel().copy()
+    e2e_plan = capi.Evolve(H, S, capi.EVOLVE_MIXED)
+    e2e_plan.run_host(hr.copy(), hi.copy(), DT, 1, s_c, m_c)   # graph recorded outside the timed region
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    capi.check(L.diaq_ham_sim_host(H.h, hpr.ctypes.data, hpi.ctypes.data, DT * args.steps, args.steps * sub, m,
-                                   opr.ctypes.data, opi.ctypes.data))
+    e2e_plan.run_host(hr, hi, DT, K, s_c, m_c)
     e2e_s = time.perf_counter() - t0
+    del e2e_plan
+
+    # ---- SpMV on its own, c128 (FP64-issue bound on GB300) ----
+    xr, xi = ppr.clone(), ppi.clone()
+    yr, yi = torch.empty_like(xr), torch.empty_like(xi)
+    for _ in range(3):
+        capi.check(L.diaq_spmv_z(H.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
+
+    def spmv_loop():
+        for i in range(args.spmv_reps):
+            a, b, c, d = (xr, xi, yr, yi) if i % 2 == 0 else (yr, yi, xr, xi)
+            capi.check(L.diaq_spmv_z(H.h, a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), sp))
+
+    spmv_us = 1e3 * _timed(stream, spmv_loop) / args.spmv_reps
 
     peak, peak_kind = peaks()
-    w = 16
-    bytes_term = w * total + 4 * w * N       # A once; term in, term out, sum read+write
-    bytes_spmv = w * total + 2 * w * N       # A once; x in, y out
-    us_term = 1e3 * ms / launches
-    achieved = bytes_term / (us_term * 1e-6) / 1e9
-    spmv_gbs = bytes_spmv / (spmv_us * 1e-6) / 1e9
-    value = world * args.steps / (ms / 1e3)
+    # algorithmic bytes of one chosen time step: per launch the c64 matrix once, per state
+    # v in (8N) + v out (8N) + sum pair read/write (16N each; the first term only writes, the
+    # last reads the pair and read-modify-writes psi in float64 instead of writing the pair)
+    chunks = (S + 7) // 8
+    per_state_step = (1 << s_c) * (m_c * 16 * N + (m_c - 1) * 16 * N + (m_c - 1) * 16 * N + 32 * N - 16 * N)
+    step_bytes = (1 << s_c) * m_c * chunks * 8 * total + S * per_state_step
+    achieved = step_bytes / (ms / K * 1e-3) / 1e9
+    value = world * S * K / (ms / 1e3)
+    plain_value = world * K / (ms_plain / 1e3)
     line = {
-        "metric": METRIC, "value": value, "unit": "states·steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded XXZ couplings and states, built in-process)",
-        "config": {"workload": f"xxz{args.n}_periodic_evolve", "form": "plain", "n_qubits": args.n, "rows": N,
-                   "ndiag": len(off), "stored_values": total, "dt": DT, "substeps": sub, "taylor_terms": m,
-                   "states_per_gpu": 1, "precision": "c128", "norm1": norm1.value,
-                   "l2": "inputs larger than L2 (matrix 654 MB c128 > 129 MB)", "parallelism": f"replicas{world}"},
+        "metric": METRIC, "value": value, "unit": "states·steps/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 terms + f64 state", "data": "synthetic (seeded XXZ couplings and states, built in-process)",
+        "config": {"workload": f"xxz{args.n}_periodic_evolve", "form": "chosen", "n_qubits": args.n, "rows": N,
+                   "ndiag": len(off), "stored_values": total, "dt": DT, "states_per_gpu": S,
+                   "substeps": 1 << s_c, "taylor_terms": m_c, "selection": "min-cost remainder bound",
+                   "tol_per_step": TOL_STEP, "norm1": norm1.value,
+                   "l2": "inputs larger than L2 (c64 matrix 327 MB, states 128 MB > 129 MB)",
+                   "parallelism": f"replicas{world}"},
+        "accuracy": {"rel_err_max": float(errs.max()), "fidelity_min": float(fid.min()),
+                     "vs": f"c128 evolution at tol 1e-14 ({1 << s_r}x{m_r} terms/step)", "steps": W + K},
+        "plain": {"value": plain_value, "ms_per_step": ms_plain / K, "substeps": 1 << s_p, "taylor_terms": m_p,
+                  "launches_per_step": lps_plain, "speedup_chosen_over_plain": value / plain_value},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "dia_spmv_kernel<double,1,EpiTaylorRhs<double>>",
-                     "bytes_per_launch": bytes_term, "us_per_launch": us_term, "peak_kind": peak_kind},
-        "spmv": {"us": spmv_us, "gbs": spmv_gbs, "frac": spmv_gbs / peak, "bytes": bytes_spmv, "reps": reps},
-        "e2e": {"value": world * args.steps / e2e_s, "unit": "states·steps/s", "h2d_bytes_per_step": 16 * N / args.steps,
-                "d2h_bytes_per_step": 16 * N / args.steps, "note": "one diaq_ham_sim_host call: psi0 up, all steps, psi down"},
+                     "traffic": None, "kernel": "dia_spmv_kernel<float,8,EpiMixed>",
+                     "bytes_per_step": step_bytes, "launches_per_step": lps, "peak_kind": peak_kind},
+        "spmv_c128": {"us": spmv_us, "gbs": (16 * total + 32 * N) / spmv_us / 1e3,
+                      "frac": (16 * total + 32 * N) / spmv_us / 1e3 / peak,
+                      "dfma_per_launch": 4 * total, "reps": args.spmv_reps},
+        "e2e": {"value": world * S * K / e2e_s, "unit": "states·steps/s", "h2d_bytes_per_step": 16 * N * S / K,
+                "d2h_bytes_per_step": 16 * N * S / K,
+                "note": "diaq_evolve_run_host: S states up, K steps, S states down, in the timed region"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
-        "norm_drift": norm_drift,
     }
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline_sample(N, off, re, im, s, m)
+        line["cpu_baseline"] = cpu_baseline_sample(N, off, re, im, s_p, m_p)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -298,6 +379,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--spmv-reps", type=int, default=1000)
+    ap.add_argument("--states", type=int, default=8, help="states evolved together by the chosen form")
+    ap.add_argument("--mode", choices=["evolve", "spmv"], default="evolve")
     ap.add_argument("--ref-steps", type=int, default=10, help="time steps the CPU reference arm times at most")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
@@ -307,6 +390,9 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.mode == "spmv":
+        run_spmv_only(args)
         return
     if world > 1:
         import torch

@@ -16,6 +16,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libdiaq_gb300.so")
 
 C128, C64 = 0, 1
+EVOLVE_C128, EVOLVE_MIXED = 0, 1
 _lib = None
 
 # name -> (restype, argtypes); mirrors include/diaq_gb300.h
@@ -47,6 +48,12 @@ SIGNATURES = {
     "diaq_ham_sim": (INT, [P, P, P, F64, I64, INT, P, P, P]),
     "diaq_ham_sim_host": (INT, [P, P, P, F64, I64, INT, P, P]),
     "diaq_select_sm": (INT, [F64, F64, F64, F64, INT, P, P]),
+    "diaq_evolve_create": (INT, [P, INT, INT, P]),
+    "diaq_evolve_destroy": (INT, [P]),
+    "diaq_evolve_run": (INT, [P, P, P, I64, F64, I64, INT, INT, P]),
+    "diaq_evolve_launches_per_step": (INT, [P]),
+    "diaq_evolve_run_host": (INT, [P, P, P, F64, I64, INT, INT]),
+    "diaq_select_sm_min_cost": (INT, [F64, F64, F64, INT, INT, P, P]),
 }
 
 
@@ -89,6 +96,13 @@ def select_sm(norm1: float, tau: float, tol: float, scale_cutoff: float = 1.0, m
     """(substeps_log2, m) of the norm-bound rule (diaq_select_sm)."""
     s, m = ctypes.c_int(), ctypes.c_int()
     check(lib().diaq_select_sm(norm1, tau, tol, scale_cutoff, max_m, ctypes.byref(s), ctypes.byref(m)))
+    return s.value, m.value
+
+
+def select_sm_min_cost(norm1: float, tau: float, tol: float, max_s: int = 12, max_m: int = 60):
+    """(substeps_log2, m) minimising 2^s * m under the same remainder bound (diaq_select_sm_min_cost)."""
+    s, m = ctypes.c_int(), ctypes.c_int()
+    check(lib().diaq_select_sm_min_cost(norm1, tau, tol, max_s, max_m, ctypes.byref(s), ctypes.byref(m)))
     return s.value, m.value
 
 
@@ -147,3 +161,28 @@ class Matrix:
 
     def prune(self):
         return self._new(lib().diaq_matrix_prune, None)
+
+
+class Evolve:
+    """Owning handle of an evolution plan (diaq_evolve_t)."""
+
+    def __init__(self, H: Matrix, nrhs: int, mode: int = EVOLVE_C128):
+        self.H = H   # the plan refers to H: keep it alive
+        out = ctypes.c_void_p()
+        check(lib().diaq_evolve_create(H.h, nrhs, mode, ctypes.byref(out)))
+        self.h = out
+
+    def run(self, psi_re, psi_im, ld, dt, steps, substeps_log2, m, stream=None):
+        check(lib().diaq_evolve_run(self.h, ptr(psi_re), ptr(psi_im), ld, dt, steps, substeps_log2, m, stream))
+
+    def run_host(self, psi_re: np.ndarray, psi_im: np.ndarray, dt, steps, substeps_log2, m):
+        """In place on host float64 arrays of nrhs*N values."""
+        check(lib().diaq_evolve_run_host(self.h, psi_re.ctypes.data, psi_im.ctypes.data, dt, steps, substeps_log2, m))
+
+    def launches_per_step(self) -> int:
+        return lib().diaq_evolve_launches_per_step(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.diaq_evolve_destroy(self.h)
+            self.h = None

@@ -100,6 +100,40 @@ int diaq_ham_sim_host(diaq_matrix_t H, const double *psi0_re, const double *psi0
 
 extern "C" {
 
+// Smallest Taylor degree k <= max_m with theta^(k+1)/(k+1)! e^theta <= budget (max_m + 1 if none).
+static int taylor_degree(double theta, double budget, int max_m) {
+    double term = theta * std::exp(theta);  // k = 0
+    for (int k = 1; k <= max_m; ++k) {
+        term *= theta / (double)(k + 1);
+        if (term <= budget) return k;
+    }
+    return max_m + 1;
+}
+
+int diaq_select_sm_min_cost(double norm1, double tau, double tol, int max_s, int max_m,
+                            int *substeps_log2, int *m) {
+    if (!substeps_log2 || !m) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    if (!(norm1 >= 0) || !(tol > 0) || max_m < 1 || max_s < 0 || max_s > 30)
+        return set_error(DIAQ_ERR_INVALID, "select_sm_min_cost: need norm1 >= 0, tol > 0, max_m >= 1, 0 <= max_s <= 30");
+    const double theta0 = std::fabs(tau) * norm1;
+    int best_s = -1, best_m = 0;
+    double best = 0.0;
+    for (int s = 0; s <= max_s; ++s) {
+        const int k = taylor_degree(std::ldexp(theta0, -s), std::ldexp(tol, -s), max_m);
+        if (k > max_m) continue;
+        const double cost = std::ldexp((double)k, s);
+        if (best_s < 0 || cost < best) {
+            best = cost;
+            best_s = s;
+            best_m = k;
+        }
+    }
+    if (best_s < 0) return set_error(DIAQ_ERR_UNSUPPORTED, "select_sm_min_cost: no (s, m) in range meets the tolerance");
+    *substeps_log2 = best_s;
+    *m = best_m;
+    return DIAQ_OK;
+}
+
 int diaq_select_sm(double norm1, double tau, double tol, double scale_cutoff, int max_m,
                    int *substeps_log2, int *m) {
     if (!substeps_log2 || !m) return set_error(DIAQ_ERR_INVALID, "NULL argument");

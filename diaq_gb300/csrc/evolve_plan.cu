@@ -1,0 +1,373 @@
+// Evolution plans: many states under one Hamiltonian, one CUDA graph per time step.
+//
+// A plan owns the work vectors for nrhs states.  run() records (once per (dt, s, m, psi), on a
+// private capture stream) a graph of one time step -- 2^s sub-steps of m Taylor-term launches,
+// each launch reading every matrix value once for all the states of a block of up to 8 -- and
+// replays it `steps` times on the caller's stream.
+//
+// Modes
+//  DIAQ_EVOLVE_C128   plain: complex128 matrix, vectors and sums (the reference's arithmetic).
+//  DIAQ_EVOLVE_MIXED  complex64 matrix and Taylor terms, the running sum of one sub-step kept as a
+//                     compensated (hi, lo) pair of floats (TwoSum per term), and the state itself
+//                     in float64: psi <- psi + (hi + lo) in double at the end of every sub-step.
+//
+// Buffers, with the terms of one step ping-ponging between two vectors (the last term of a
+// sub-step writes the next sub-step's first input, fp32(psi), into the buffer the term would
+// have used):
+//   C128:  psi (caller's), sum, term_a, term_b                 (float64)
+//   MIXED: psi (caller's, float64); v_a, v_b, hi, lo           (float32)
+#include <cmath>
+#include <map>
+#include <tuple>
+
+#include "spmv_kernel.cuh"
+
+namespace diaq_gb300 {
+
+// ---- epilogues ---------------------------------------------------------------------------------------
+// Plain term: term = (-i*scale) * (A x); out = base + term, base = init (first term) or `in`.
+struct EpiPlain {
+    double *tr, *ti;              // term out (NULL on a sub-step's last term: nobody reads it)
+    const double *br, *bi;        // base of the sum
+    double *outr, *outi;          // sum out
+    int64_t ld;
+    double scale;
+    EpiPlain shifted(int q0) const {
+        EpiPlain e = *this;
+        const int64_t o = q0 * ld;
+        if (e.tr) {
+            e.tr += o;
+            e.ti += o;
+        }
+        e.br += o;
+        e.bi += o;
+        e.outr += o;
+        e.outi += o;
+        return e;
+    }
+    template <typename U, int K, int V>
+    __device__ __forceinline__ void apply(int64_t r0, int64_t rows, int kq, U (&sr)[K][V], U (&si)[K][V]) const {
+#pragma unroll
+        for (int q = 0; q < K; ++q)
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int64_t r = r0 + v;
+                if (q < kq && r < rows) {
+                    const int64_t i = q * ld + r;
+                    const double nr = si[q][v] * scale, ni = -sr[q][v] * scale;
+                    if (tr) {
+                        tr[i] = nr;
+                        ti[i] = ni;
+                    }
+                    outr[i] = br[i] + nr;
+                    outi[i] = bi[i] + ni;
+                }
+            }
+    }
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Mixed term k of a sub-step: t = (-i*scale) * (A v) in float32;
+//   k == 1:  hi = t, lo = 0;  else (hi, e) = TwoSum(hi, t), lo += e;
+//   k <  m:  vout = t;
+//   k == m:  psi += (double)hi + (double)lo;  vout = fp32(psi)  (next sub-step's input).
+struct EpiMixed {
+    float *vr, *vi;                     // vout
+    float *hr, *hi_, *lr, *li;          // compensated sum (hi, lo), re and im
+    double *pr, *pi;                    // state
+    int64_t ld;
+    float scale;
+    int first, last;
+    EpiMixed shifted(int q0) const {
+        EpiMixed e = *this;
+        const int64_t o = q0 * ld;
+        e.vr += o;
+        e.vi += o;
+        e.hr += o;
+        e.hi_ += o;
+        e.lr += o;
+        e.li += o;
+        e.pr += o;
+        e.pi += o;
+        return e;
+    }
+    template <typename U, int K, int V>
+    __device__ __forceinline__ void apply(int64_t r0, int64_t rows, int kq, U (&sr)[K][V], U (&si)[K][V]) const {
+#pragma unroll
+        for (int q = 0; q < K; ++q)
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int64_t r = r0 + v;
+                if (q >= kq || r >= rows) continue;
+                const int64_t i = q * ld + r;
+                const float tr = si[q][v] * scale, ti = -sr[q][v] * scale;
+                float h_r, h_i, l_r, l_i;
+                if (first) {
+                    h_r = tr;
+                    h_i = ti;
+                    l_r = 0.f;
+                    l_i = 0.f;
+                } else {
+                    float e_r, e_i;
+                    two_sum(hr[i], tr, h_r, e_r);
+                    two_sum(hi_[i], ti, h_i, e_i);
+                    l_r = lr[i] + e_r;
+                    l_i = li[i] + e_i;
+                }
+                if (!last) {
+                    hr[i] = h_r;
+                    hi_[i] = h_i;
+                    lr[i] = l_r;
+                    li[i] = l_i;
+                    vr[i] = tr;
+                    vi[i] = ti;
+                } else {
+                    const double nr = pr[i] + ((double)h_r + (double)l_r);
+                    const double ni = pi[i] + ((double)h_i + (double)l_i);
+                    pr[i] = nr;
+                    pi[i] = ni;
+                    vr[i] = (float)nr;
+                    vi[i] = (float)ni;
+                }
+            }
+    }
+};
+
+__global__ void to_f32_kernel(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+// ---- the plan ------------------------------------------------------------------------------------------
+struct EvolvePlan {
+    const Matrix *H = nullptr;   // the caller's matrix (c128)
+    Matrix *Hc = nullptr;        // owned c64 copy (MIXED)
+    int mode = 0, nrhs = 1;
+    int64_t n = 0;
+    void *buf = nullptr;         // work vectors
+    cudaStream_t s = nullptr;    // capture stream
+    struct Key {
+        double dt;
+        int sl, m;
+        double *pr, *pi;
+        int64_t ld;
+        bool operator<(const Key &o) const {
+            return std::tie(dt, sl, m, pr, pi, ld) < std::tie(o.dt, o.sl, o.m, o.pr, o.pi, o.ld);
+        }
+    };
+    std::map<Key, cudaGraphExec_t> graphs;
+    int launches_per_step = 0;
+
+    ~EvolvePlan() {
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        if (buf) cudaFree(buf);
+        if (Hc) destroy(Hc);
+        if (s) cudaStreamDestroy(s);
+    }
+};
+
+}  // namespace diaq_gb300
+
+// The public handle is the plan itself; every plan is allocated as one.
+struct diaq_evolve_s : public diaq_gb300::EvolvePlan {};
+
+namespace diaq_gb300 {
+
+static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
+    if (H.rows != H.cols) return set_error(DIAQ_ERR_INVALID, "evolve: H must be square");
+    if (H.prec != DIAQ_C128) return set_error(DIAQ_ERR_INVALID, "evolve: pass the c128 matrix (the plan makes its own c64 copy)");
+    if (nrhs < 1) return set_error(DIAQ_ERR_INVALID, "evolve: nrhs must be >= 1");
+    if (mode != DIAQ_EVOLVE_C128 && mode != DIAQ_EVOLVE_MIXED) return set_error(DIAQ_ERR_INVALID, "evolve: unknown mode");
+    EvolvePlan *P = new diaq_evolve_s();
+    P->H = &H;
+    P->mode = mode;
+    P->nrhs = nrhs;
+    P->n = H.rows;
+    int st = DIAQ_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&P->s, cudaStreamNonBlocking);
+    const size_t vec = (size_t)nrhs * (size_t)P->n;
+    const size_t bytes = mode == DIAQ_EVOLVE_C128 ? 6 * vec * sizeof(double) : 8 * vec * sizeof(float);
+    if (e == cudaSuccess && bytes) e = cudaMalloc(&P->buf, bytes);
+    if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
+    if (st == DIAQ_OK && mode == DIAQ_EVOLVE_MIXED) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
+    if (st != DIAQ_OK) {
+        delete static_cast<diaq_evolve_s *>(P);
+        return st;
+    }
+    *out = P;
+    return DIAQ_OK;
+}
+
+// Enqueue one time step on P->s (used under stream capture).
+static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, double *pi, int64_t ld) {
+    const int64_t n = P.n, k = P.nrhs;
+    const int sub = 1 << sl;
+    const double tau = dt / (double)sub;
+    P.launches_per_step = 0;
+    if (P.mode == DIAQ_EVOLVE_C128) {
+        double *w = (double *)P.buf;
+        const int64_t L = n;  // work vectors use ld = n
+        double *sr = w, *si = w + k * L, *ar = w + 2 * k * L, *ai = w + 3 * k * L, *br = w + 4 * k * L,
+               *bi = w + 5 * k * L;
+        // work vectors have leading dimension n; the caller's psi uses ld.  The first term of a
+        // sub-step reads psi; keep the caller's layout by requiring ld == n here.
+        if (ld != n) return set_error(DIAQ_ERR_UNSUPPORTED, "evolve c128: psi leading dimension must equal N");
+        double *cur_r = pr, *cur_i = pi, *oth_r = sr, *oth_i = si;
+        for (int j = 0; j < sub; ++j) {
+            const double *tin_r = cur_r, *tin_i = cur_i;
+            double *tout_r = ar, *tout_i = ai;
+            for (int t = 1; t <= m; ++t) {
+                EpiPlain e;
+                const bool last = (t == m);
+                e.tr = last ? nullptr : tout_r;
+                e.ti = last ? nullptr : tout_i;
+                e.br = (t == 1) ? cur_r : oth_r;
+                e.bi = (t == 1) ? cur_i : oth_i;
+                e.outr = oth_r;
+                e.outi = oth_i;
+                e.ld = L;
+                e.scale = tau / (double)t;
+                DQ_TRY(launch_dia_spmv_rhs<double>(*P.H, tin_r, tin_i, L, (int)k, e, P.s));
+                ++P.launches_per_step;
+                tin_r = tout_r;
+                tin_i = tout_i;
+                tout_r = (tout_r == ar) ? br : ar;
+                tout_i = (tout_i == ai) ? bi : ai;
+            }
+            if (m == 0) continue;
+            std::swap(cur_r, oth_r);
+            std::swap(cur_i, oth_i);
+        }
+        if (cur_r != pr) {
+            DQ_CUDA(cudaMemcpyAsync(pr, cur_r, sizeof(double) * k * L, cudaMemcpyDeviceToDevice, P.s));
+            DQ_CUDA(cudaMemcpyAsync(pi, cur_i, sizeof(double) * k * L, cudaMemcpyDeviceToDevice, P.s));
+        }
+        return DIAQ_OK;
+    }
+    // MIXED
+    float *w = (float *)P.buf;
+    const int64_t L = n;
+    if (ld != n) return set_error(DIAQ_ERR_UNSUPPORTED, "evolve mixed: psi leading dimension must equal N");
+    float *var = w, *vai = w + k * L, *vbr = w + 2 * k * L, *vbi = w + 3 * k * L;
+    float *hr = w + 4 * k * L, *hi = w + 5 * k * L, *lr = w + 6 * k * L, *li = w + 7 * k * L;
+    float *in_r = var, *in_i = vai, *out_r = vbr, *out_i = vbi;  // v_a holds fp32(psi) on entry
+    for (int j = 0; j < sub; ++j) {
+        for (int t = 1; t <= m; ++t) {
+            EpiMixed e;
+            e.vr = out_r;
+            e.vi = out_i;
+            e.hr = hr;
+            e.hi_ = hi;
+            e.lr = lr;
+            e.li = li;
+            e.pr = pr;
+            e.pi = pi;
+            e.ld = L;
+            e.scale = (float)(tau / (double)t);
+            e.first = (t == 1);
+            e.last = (t == m);
+            DQ_TRY(launch_dia_spmv_rhs<float>(*P.Hc, in_r, in_i, L, (int)k, e, P.s));
+            ++P.launches_per_step;
+            std::swap(in_r, out_r);
+            std::swap(in_i, out_i);
+        }
+    }
+    if (in_r != var) {  // an odd number of launches: put fp32(psi) back where the next step reads it
+        DQ_CUDA(cudaMemcpyAsync(var, in_r, sizeof(float) * k * L, cudaMemcpyDeviceToDevice, P.s));
+        DQ_CUDA(cudaMemcpyAsync(vai, in_i, sizeof(float) * k * L, cudaMemcpyDeviceToDevice, P.s));
+    }
+    return DIAQ_OK;
+}
+
+static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt, int64_t steps, int sl, int m,
+                    cudaStream_t user) {
+    if (steps < 0 || m < 0 || sl < 0 || sl > 20) return set_error(DIAQ_ERR_INVALID, "evolve: bad steps / s / m");
+    if (!pr || !pi) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
+    if (steps == 0 || m == 0 || P.n == 0) return DIAQ_OK;
+    const EvolvePlan::Key key{dt, sl, m, pr, pi, ld};
+    auto it = P.graphs.find(key);
+    if (it == P.graphs.end()) {
+        // record one step on the plan's own stream (capture needs a stream other than the
+        // legacy default); nothing runs during capture
+        cudaGraph_t g = nullptr;
+        DQ_CUDA(cudaStreamBeginCapture(P.s, cudaStreamCaptureModeThreadLocal));
+        const int st = enqueue_step(P, dt, sl, m, pr, pi, ld);
+        cudaError_t e = cudaStreamEndCapture(P.s, &g);
+        if (st != DIAQ_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        cudaGraphExec_t ge = nullptr;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+        it = P.graphs.emplace(key, ge).first;
+    }
+    // everything below runs on the caller's stream
+    if (P.mode == DIAQ_EVOLVE_MIXED) {  // fp32(psi) into v_a for the first sub-step
+        float *var = (float *)P.buf, *vai = var + P.nrhs * P.n;
+        const int64_t cnt = P.nrhs * P.n;
+        const int grid = (int)std::min<int64_t>((cnt + 255) / 256, 8 * num_sms());
+        to_f32_kernel<<<grid, 256, 0, user>>>(pr, var, cnt);
+        to_f32_kernel<<<grid, 256, 0, user>>>(pi, vai, cnt);
+        DQ_CUDA(cudaGetLastError());
+    }
+    for (int64_t i = 0; i < steps; ++i) DQ_CUDA(cudaGraphLaunch(it->second, user));
+    return DIAQ_OK;
+}
+
+}  // namespace diaq_gb300
+
+using namespace diaq_gb300;
+
+extern "C" {
+
+int diaq_evolve_create(diaq_matrix_t H, int nrhs, int mode, diaq_evolve_t *out) {
+    if (!H || !out) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    EvolvePlan *P = nullptr;
+    DQ_TRY(plan_create(*H, nrhs, mode, &P));
+    *out = static_cast<diaq_evolve_t>(P);
+    return DIAQ_OK;
+}
+
+int diaq_evolve_destroy(diaq_evolve_t E) {
+    delete E;
+    return DIAQ_OK;
+}
+
+int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld, double dt, int64_t steps,
+                    int substeps_log2, int m, void *stream) {
+    if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
+    return plan_run(*E, psi_re, psi_im, ld, dt, steps, substeps_log2, m, (cudaStream_t)stream);
+}
+
+int diaq_evolve_launches_per_step(diaq_evolve_t E) { return E ? E->launches_per_step : 0; }
+
+int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
+                         int substeps_log2, int m) {
+    if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
+    if (!psi_re || !psi_im) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
+    const size_t cnt = (size_t)E->nrhs * (size_t)E->n;
+    if (cnt == 0) return DIAQ_OK;
+    double *d = nullptr;
+    DQ_CUDA(cudaMalloc(&d, 2 * cnt * sizeof(double)));
+    cudaError_t e = cudaMemcpy(d, psi_re, cnt * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + cnt, psi_im, cnt * sizeof(double), cudaMemcpyHostToDevice);
+    int st = e == cudaSuccess ? DIAQ_OK : cuda_status(e, "evolve upload", __FILE__, __LINE__);
+    if (st == DIAQ_OK) st = plan_run(*E, d, d + cnt, E->n, dt, steps, substeps_log2, m, nullptr);
+    if (st == DIAQ_OK) {
+        e = cudaMemcpy(psi_re, d, cnt * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(psi_im, d + cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = cuda_status(e, "evolve download", __FILE__, __LINE__);
+    }
+    cudaFree(d);
+    return st;
+}
+
+}  // extern "C"

@@ -72,7 +72,7 @@ template <typename T, int K, class Epi>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_kernel(const DiagMeta *__restrict__ meta, int nd, const T *__restrict__ are,
                     const T *__restrict__ aim, int64_t rows, const T *__restrict__ xr,
-                    const T *__restrict__ xi, int64_t ldx, Epi epi) {
+                    const T *__restrict__ xi, int64_t ldx, int kq, Epi epi) {
     constexpr int V = VecOf<T>::V;
     __shared__ DiagMeta sm[kMetaChunk];
     const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
@@ -106,6 +106,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
             const int64_t c = r0 + d;
 #pragma unroll
             for (int q = 0; q < K; ++q) {
+                if (q >= kq) break;
                 const T *pxr = xr + q * ldx + c;
                 const T *pxi = xi + q * ldx + c;
                 T xrv[V], xiv[V];
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
             }
         }
     }
-    if (r0 < rows) epi.template apply<T, K, V>(r0, rows, accr, acci);
+    if (r0 < rows) epi.template apply<T, K, V>(r0, rows, kq, accr, acci);
 }
 
 // Store y = A x.
@@ -139,9 +140,10 @@ struct EpiStore {
     T *yr, *yi;
     int64_t ldy;
     template <typename U, int K, int V>
-    __device__ __forceinline__ void apply(int64_t r0, int64_t rows, U (&ar)[K][V], U (&ai)[K][V]) const {
+    __device__ __forceinline__ void apply(int64_t r0, int64_t rows, int kq, U (&ar)[K][V], U (&ai)[K][V]) const {
 #pragma unroll
         for (int q = 0; q < K; ++q) {
+            if (q >= kq) break;
             T *pr = yr + q * ldy + r0, *pi = yi + q * ldy + r0;
             if (r0 + V <= rows && aligned16(pr) && aligned16(pi)) {
                 using VT = typename VecOf<T>::type;
@@ -179,13 +181,13 @@ struct EpiTaylor {
     int64_t ld;
     T scale;
     template <typename U, int K, int V>
-    __device__ __forceinline__ void apply(int64_t r0, int64_t rows, U (&sr)[K][V], U (&si)[K][V]) const {
+    __device__ __forceinline__ void apply(int64_t r0, int64_t rows, int kq, U (&sr)[K][V], U (&si)[K][V]) const {
 #pragma unroll
         for (int q = 0; q < K; ++q)
 #pragma unroll
             for (int v = 0; v < V; ++v) {
                 const int64_t r = r0 + v;
-                if (r < rows) {
+                if (q < kq && r < rows) {
                     const int64_t i = q * ld + r;
                     const T a = sr[q][v], b = si[q][v];
                     const T nr = b * scale, ni = -a * scale;
@@ -208,7 +210,8 @@ inline unsigned spmv_blocks(int64_t rows, int V) {
     return (unsigned)((rows + per - 1) / per);
 }
 
-// Launch with the right-hand sides in chunks of 8/4/2/1; Epi must offer `shifted(q0)`, the
+// Launch over the right-hand sides in chunks of up to 8 (one matrix read per chunk, the kernel
+// instantiated for 1, 2, 4 or 8 with the unused slots masked); Epi must offer `shifted(q0)`, the
 // same epilogue for right-hand sides q0.. .
 template <typename T, class Epi>
 int launch_dia_spmv_rhs(const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, Epi epi,
@@ -219,25 +222,22 @@ int launch_dia_spmv_rhs(const Matrix &A, const T *xr, const T *xi, int64_t ldx, 
     int q0 = 0;
     while (q0 < nrhs) {
         const int left = nrhs - q0;
+        const int kq = left < 8 ? left : 8;  // states in this launch; the matrix is read once for them
         const T *pxr = xr + q0 * ldx, *pxi = xi + q0 * ldx;
         const Epi e = epi.shifted(q0);
-        if (left >= 8) {
+        if (kq > 4)
             dia_spmv_kernel<T, 8, Epi><<<grid, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const T *)A.re, (const T *)A.im,
-                                                                     A.rows, pxr, pxi, ldx, e);
-            q0 += 8;
-        } else if (left >= 4) {
+                                                                     A.rows, pxr, pxi, ldx, kq, e);
+        else if (kq > 2)
             dia_spmv_kernel<T, 4, Epi><<<grid, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const T *)A.re, (const T *)A.im,
-                                                                     A.rows, pxr, pxi, ldx, e);
-            q0 += 4;
-        } else if (left >= 2) {
+                                                                     A.rows, pxr, pxi, ldx, kq, e);
+        else if (kq == 2)
             dia_spmv_kernel<T, 2, Epi><<<grid, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const T *)A.re, (const T *)A.im,
-                                                                     A.rows, pxr, pxi, ldx, e);
-            q0 += 2;
-        } else {
+                                                                     A.rows, pxr, pxi, ldx, kq, e);
+        else
             dia_spmv_kernel<T, 1, Epi><<<grid, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const T *)A.re, (const T *)A.im,
-                                                                     A.rows, pxr, pxi, ldx, e);
-            q0 += 1;
-        }
+                                                                     A.rows, pxr, pxi, ldx, kq, e);
+        q0 += kq;
     }
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;

@@ -41,7 +41,14 @@ typedef enum {
     DIAQ_C64 = 1   /* complex float, SoA float32 */
 } diaq_precision;
 
+typedef enum {
+    DIAQ_EVOLVE_C128 = 0, /* complex128 throughout (the reference's arithmetic) */
+    DIAQ_EVOLVE_MIXED = 1 /* complex64 matrix and Taylor terms, compensated float sums,
+                             float64 state */
+} diaq_evolve_mode;
+
 typedef struct diaq_matrix_s *diaq_matrix_t;
+typedef struct diaq_evolve_s *diaq_evolve_t;
 
 /* Message of the last failing call on this thread ("" if none). */
 const char *diaq_last_error(void);
@@ -175,12 +182,41 @@ int diaq_expm(diaq_matrix_t A, int max_iterations, double scale_cutoff, double t
 int diaq_ham_sim(diaq_matrix_t H, const double *psi0_re, const double *psi0_im, double t,
                  int64_t r, int max_iterations, double *psi_re, double *psi_im, void *stream);
 
+/* An evolution plan for nrhs states under H (a c128 matrix; mode DIAQ_EVOLVE_MIXED keeps its own
+ * c64 copy) with the work vectors it needs.  No counterpart in the reference, whose
+ * hamiltonian_simulation_cuda (src/spHamSim_gpu_all_fused.cu:287-376) evolves one state with a
+ * fixed number of terms and no sub-steps; with nrhs = 1, mode C128, 2^s = 1 and m =
+ * max_iterations a plan computes the same thing. */
+int diaq_evolve_create(diaq_matrix_t H, int nrhs, int mode, diaq_evolve_t *out);
+
+int diaq_evolve_destroy(diaq_evolve_t E);
+
+/* Advance the nrhs states in place by `steps` time steps of dt, each 2^substeps_log2 sub-steps
+ * of m Taylor terms.  psi_re/psi_im: float64 device arrays, state q at psi[q*ld ..]; ld must be
+ * N.  The first call for a given (dt, s, m, psi) records one step as a CUDA graph; every step is
+ * a replay.  Asynchronous on stream. */
+int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld, double dt,
+                    int64_t steps, int substeps_log2, int m, void *stream);
+
+/* diaq_evolve_run with host arrays: the nrhs states (state q at psi[q*N ..]) are copied to the
+ * device, advanced, and copied back.  Synchronous. */
+int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
+                         int substeps_log2, int m);
+
+/* Kernel launches in one recorded time step of the last graph built (0 before any run). */
+int diaq_evolve_launches_per_step(diaq_evolve_t E);
+
 /* Norm-bound choice of the sub-step count and Taylor degree for one time step tau: the
  * reference's scaling rule s = ceil(log2(tau*norm1/cutoff)) (src/spME.cpp:256-262) gives 2^s
  * sub-steps of theta = tau*norm1/2^s each, and m is the smallest degree whose Taylor remainder
  * bound theta^(m+1)/(m+1)! * exp(theta) is <= tol / 2^s (capped at max_m).  Host-only. */
 int diaq_select_sm(double norm1, double tau, double tol, double scale_cutoff, int max_m,
                    int *substeps_log2, int *m);
+
+/* The cheapest (2^s * m) pair whose remainder bound meets tol (per step, split over the 2^s
+ * sub-steps as in diaq_select_sm), searching s = 0..max_s.  Host-only. */
+int diaq_select_sm_min_cost(double norm1, double tau, double tol, int max_s, int max_m,
+                            int *substeps_log2, int *m);
 
 /* diaq_ham_sim with host vectors (psi0 uploaded once, the result downloaded once), as
  * hamiltonian_simulation_cuda does.  Synchronous. */

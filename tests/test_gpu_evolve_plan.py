@@ -1,0 +1,102 @@
+"""Evolution plans (graph-captured steps, several states per launch): plain c128 against the
+oracle at 1e-12, the mixed-precision form against the FP64 oracle at the 1e-6 bar."""
+import numpy as np
+import pytest
+
+from conftest import maxrel
+from diaq_gb300 import hamiltonians as ham
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(capi, n, k, mode, model="xxz"):
+    import torch
+
+    N, off, re, im = ham.xxz(n) if model == "xxz" else ham.tfim(n)
+    H = capi.Matrix.create(N, N, off, re, im)
+    E = capi.Evolve(H, k, mode)
+    P = ham.random_state(N, 0, k=k) if k > 1 else ham.random_state(N, 0)[None, :]
+    pr = torch.from_numpy(np.ascontiguousarray(P.real)).cuda()
+    pi = torch.from_numpy(np.ascontiguousarray(P.imag)).cuda()
+    return orc.OMatrix(N, N, off, re, im), E, P, pr, pi
+
+
+def _result(pr, pi):
+    import torch
+
+    torch.cuda.synchronize()
+    return (pr + 1j * pi).cpu().numpy()
+
+
+@pytest.mark.parametrize("sl,m", [(0, 14), (1, 9), (2, 6), (0, 1), (1, 1)])
+def test_plain_matches_oracle(native, sl, m):
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 12, 3, capi.EVOLVE_C128)
+    E.run(pr, pi, A.rows, 0.05, 4, sl, m)
+    got = _result(pr, pi)
+    for q in range(3):
+        want = orc.ham_sim(A, P[q], 0.05 * 4, 4, m, substeps=1 << sl)
+        assert maxrel(got[q], want) < 1e-12, q
+    assert E.launches_per_step() == (1 << sl) * m * 1   # 3 states share each launch
+
+
+def test_plain_single_state_equals_reference_rule(native):
+    """nrhs = 1, no sub-steps, m = max_iterations: the reference's hamiltonian_simulation_cuda."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 10, 1, capi.EVOLVE_C128, "tfim")
+    E.run(pr, pi, A.rows, 0.1, 5, 0, 20)
+    assert maxrel(_result(pr, pi)[0], orc.ham_sim(A, P[0], 0.5, 5, 20)) < 1e-12
+
+
+def test_plain_many_states_chunks(native):
+    """More than 8 states: launches run in chunks of 8 right-hand sides."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 10, 11, capi.EVOLVE_C128)
+    E.run(pr, pi, A.rows, 0.05, 3, 1, 8)
+    got = _result(pr, pi)
+    for q in (0, 7, 8, 10):
+        assert maxrel(got[q], orc.ham_sim(A, P[q], 0.15, 3, 8, substeps=2)) < 1e-12
+
+
+@pytest.mark.parametrize("k", [1, 4, 8])
+def test_mixed_accuracy(native, k):
+    """complex64 terms, compensated float sums, float64 state: within 1e-6 of the FP64 oracle
+    after 20 steps of dt = 0.05 (the same (s, m))."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 12, k, capi.EVOLVE_MIXED)
+    E.run(pr, pi, A.rows, 0.05, 20, 1, 12)
+    got = _result(pr, pi)
+    for q in range(k):
+        want = orc.ham_sim(A, P[q], 1.0, 20, 12, substeps=2)
+        err = np.linalg.norm(got[q] - want) / np.linalg.norm(want)
+        assert err < 1e-6, (q, err)
+
+
+def test_mixed_odd_launch_count(native):
+    """s = 0 and odd m: the step ends with one copy so the next replay finds fp32(psi)."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 10, 2, capi.EVOLVE_MIXED)
+    E.run(pr, pi, A.rows, 0.02, 6, 0, 11)
+    got = _result(pr, pi)
+    want = orc.ham_sim(A, P[1], 0.12, 6, 11)
+    assert np.linalg.norm(got[1] - want) / np.linalg.norm(want) < 1e-6
+
+
+def test_repeated_runs_reuse_graph(native):
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 10, 2, capi.EVOLVE_C128)
+    for _ in range(3):
+        E.run(pr, pi, A.rows, 0.05, 2, 0, 10)
+    got = _result(pr, pi)
+    assert maxrel(got[0], orc.ham_sim(A, P[0], 0.3, 6, 10)) < 1e-12
+
+
+def test_plan_rejects_bad_input(native):
+    capi, _ = native
+    M = capi.Matrix.create(4, 6, [0], np.ones(4), np.zeros(4))
+    with pytest.raises(capi.DiaqError, match="square"):
+        capi.Evolve(M, 1)
+    S = capi.Matrix.create(4, 4, [0], np.ones(4), np.zeros(4), precision=capi.C64)
+    with pytest.raises(capi.DiaqError, match="c128"):
+        capi.Evolve(S, 1)
