@@ -112,9 +112,13 @@ def plain_schedule(capi, norm1: float):
 
 # ---- reference arm: the CPU restatement -------------------------------------------------------------
 def run_reference(args, rank):
+    """The reference's own CPU code where it was built on this host (oracle/_ref, x86 builds of
+    the reference sources), else the C restatement of the same algorithm (the GPU hosts, which
+    do not have the reference sources)."""
     if rank != 0:
         return
     from oracle import oracle as orc
+    from oracle import reference as ref
     from diaq_gb300 import hamiltonians as ham
 
     N, off, re, im = workload(args.n)
@@ -124,25 +128,37 @@ def run_reference(args, rank):
     psi = ham.random_state(N, 0)
     steps = max(1, min(args.steps, args.ref_steps))
     warm = min(args.warmup, 1)
+    kind, cores = "port", orc.threads()
+    step = lambda p: orc.ham_sim(H, p, DT, 1, m, substeps=1 << s)
+    try:
+        if ref.available():
+            ref.lib()
+            kind, cores = "reference", ref.lib().ref_threads()
+            step = lambda p: ref.ham_sim(H, p, DT, 1 << s, m)
+    except OSError:
+        pass
     for _ in range(warm):
-        psi = orc.ham_sim(H, psi, DT, 1, m, substeps=1 << s)
+        psi = step(psi)
     t0 = time.perf_counter()
     for _ in range(steps):
-        psi = orc.ham_sim(H, psi, DT, 1, m, substeps=1 << s)
+        psi = step(psi)
     wall = time.perf_counter() - t0
     value = steps / wall
+    what = ("the reference's CPU spMV (src/spMV.cpp) driving the time-evolution rule"
+            if kind == "reference" else "C/OpenMP restatement (oracle port)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "states·steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * wall / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"xxz{args.n}_periodic_evolve", "n_qubits": args.n, "rows": N, "ndiag": len(off),
                    "dt": DT, "substeps": 1 << s, "taylor_terms": m, "states": 1},
-        "cpu_baseline": {"value": value, "unit": "states·steps/s", "cores": orc.threads(), "kind": "port",
-                         "sample": f"{steps} time step(s) of one state, {1 << s}x{m} SpMVs each, C/OpenMP restatement"},
+        "cpu_baseline": {"value": value, "unit": "states·steps/s", "cores": cores, "kind": kind,
+                         "sample": f"{steps} time step(s) of one state, {1 << s}x{m} SpMVs each, {what}"},
         "e2e": {"value": value, "unit": "states·steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "reference CPU code cannot be built on this host (its sources are not shipped); the oracle "
-                "port of the same algorithm is timed",
     }
+    if kind == "port":
+        line["note"] = ("the reference's CPU sources are not on this host, so its CPU library cannot be built "
+                        "here; the C restatement of the same algorithm is timed")
     print(json.dumps(line), flush=True)
 
 
@@ -246,6 +262,32 @@ def run_spmv_only(args):
         by = w * int(re.size) + 2 * w * N
         out[name] = {"us": us, "gbs": by / us / 1e3, "bytes": by}
     print(json.dumps({"mode": "spmv", "n_qubits": args.n, **out}), flush=True)
+
+
+def run_chosen_only(args):
+    """Only the chosen form's evolution, W + K steps (a light command for profilers)."""
+    import torch
+
+    from diaq_gb300 import build, capi
+    from diaq_gb300 import hamiltonians as ham
+
+    build.build()
+    L = capi.lib()
+    N, off, re, im = workload(args.n)
+    H = capi.Matrix.create(N, N, off, re, im)
+    norm1 = ctypes.c_double()
+    capi.check(L.diaq_norm1_est(H.h, ctypes.byref(norm1), None))
+    s_c, m_c = capi.select_sm_min_cost(norm1.value, DT, TOL_STEP, 12, 60)
+    E = capi.Evolve(H, args.states, capi.EVOLVE_MIXED)
+    P0 = ham.random_state(N, 0, k=args.states) if args.states > 1 else ham.random_state(N, 0)[None, :]
+    pr = torch.from_numpy(np.ascontiguousarray(P0.real)).cuda()
+    pi = torch.from_numpy(np.ascontiguousarray(P0.imag)).cuda()
+    sp = torch.cuda.current_stream().cuda_stream
+    E.run(pr, pi, N, DT, args.warmup, s_c, m_c, sp)
+    ms = _timed(torch.cuda.current_stream(), lambda: E.run(pr, pi, N, DT, args.steps, s_c, m_c, sp))
+    print(json.dumps({"mode": "chosen", "n_qubits": args.n, "states": args.states, "s": s_c, "m": m_c,
+                      "ms_per_step": ms / args.steps, "us_per_launch": 1e3 * ms / args.steps / E.launches_per_step()}),
+          flush=True)
 
 
 def run_ours(args, rank, world):
@@ -380,7 +422,9 @@ def main():
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--spmv-reps", type=int, default=1000)
     ap.add_argument("--states", type=int, default=8, help="states evolved together by the chosen form")
-    ap.add_argument("--mode", choices=["evolve", "spmv"], default="evolve")
+    ap.add_argument("--mode", choices=["evolve", "spmv", "chosen"], default="evolve",
+                    help="evolve: the full measurement; spmv: the SpMV kernel alone; chosen: only the chosen "
+                         "form's evolution (for profiling)")
     ap.add_argument("--ref-steps", type=int, default=10, help="time steps the CPU reference arm times at most")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
@@ -393,6 +437,9 @@ def main():
         return
     if args.mode == "spmv":
         run_spmv_only(args)
+        return
+    if args.mode == "chosen":
+        run_chosen_only(args)
         return
     if world > 1:
         import torch

@@ -54,6 +54,16 @@ SIGNATURES = {
     "diaq_evolve_launches_per_step": (INT, [P]),
     "diaq_evolve_run_host": (INT, [P, P, P, F64, I64, INT, INT]),
     "diaq_select_sm_min_cost": (INT, [F64, F64, F64, INT, INT, P, P]),
+    "diaq_matrix_from_pauli": (INT, [INT, I32, P, P, P, P, INT, P, P]),
+    "diaq_mlp_num_params": (INT, []),
+    "diaq_mlp_create": (INT, [ctypes.c_uint64, P]),
+    "diaq_mlp_destroy": (INT, [P]),
+    "diaq_mlp_get_params": (INT, [P, P]),
+    "diaq_mlp_set_params": (INT, [P, P]),
+    "diaq_mlp_forward": (INT, [P, P, INT, P, P]),
+    "diaq_mlp_gradient": (INT, [P, P, P, P, INT, P, P, P]),
+    "diaq_mlp_train_step": (INT, [P, P, P, P, INT, ctypes.c_float, P, P]),
+    "diaq_mlp_propose": (INT, [P, P, INT, P, P, P]),
 }
 
 
@@ -148,6 +158,18 @@ class Matrix:
         check(lib().diaq_matrix_download(self.h, re.ctypes.data, im.ctypes.data, 0, None))
         return self.offsets(), re[:total], im[:total]
 
+    @staticmethod
+    def from_pauli(n_qubits: int, coeffs, x_masks, z_masks, precision=C128, stream=None) -> "Matrix":
+        """H = sum_k c_k P_k from Pauli strings (masks over the basis index, qubit 0 = top bit)."""
+        c = np.asarray(coeffs, dtype=np.complex128)
+        cr, ci = np.ascontiguousarray(c.real), np.ascontiguousarray(c.imag)
+        xm = np.ascontiguousarray(x_masks, dtype=np.uint64)
+        zm = np.ascontiguousarray(z_masks, dtype=np.uint64)
+        out = ctypes.c_void_p()
+        check(lib().diaq_matrix_from_pauli(n_qubits, len(c), cr.ctypes.data, ci.ctypes.data, xm.ctypes.data,
+                                           zm.ctypes.data, precision, stream, ctypes.byref(out)))
+        return Matrix(out)
+
     def _new(self, fn, *args) -> "Matrix":
         out = ctypes.c_void_p()
         check(fn(self.h, *args, ctypes.byref(out)))
@@ -186,3 +208,42 @@ class Evolve:
         if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
             _lib.diaq_evolve_destroy(self.h)
             self.h = None
+
+
+class Mlp:
+    """Owning handle of the (s, m) proposer network (diaq_mlp_t); tensors are torch CUDA tensors."""
+
+    N_IN, N_S, N_M = 16, 21, 30
+
+    def __init__(self, seed: int = 0):
+        out = ctypes.c_void_p()
+        check(lib().diaq_mlp_create(seed, ctypes.byref(out)))
+        self.h = out
+        self.n_params = lib().diaq_mlp_num_params()
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.diaq_mlp_destroy(self.h)
+            self.h = None
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.n_params, dtype=np.float32)
+        check(lib().diaq_mlp_get_params(self.h, p.ctypes.data))
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        check(lib().diaq_mlp_set_params(self.h, p.ctypes.data))
+
+    def forward(self, X, logits, stream=None):
+        check(lib().diaq_mlp_forward(self.h, ptr(X), X.shape[0], ptr(logits), stream))
+
+    def gradient(self, X, ys, ym, grad, loss, stream=None):
+        check(lib().diaq_mlp_gradient(self.h, ptr(X), ptr(ys), ptr(ym), X.shape[0], ptr(grad), ptr(loss), stream))
+
+    def train_step(self, X, ys, ym, lr, loss=None, stream=None):
+        check(lib().diaq_mlp_train_step(self.h, ptr(X), ptr(ys), ptr(ym), X.shape[0], lr, ptr(loss), stream))
+
+    def propose(self, X, s_out, m_out, stream=None):
+        check(lib().diaq_mlp_propose(self.h, ptr(X), X.shape[0], ptr(s_out), ptr(m_out), stream))

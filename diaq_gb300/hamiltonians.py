@@ -172,3 +172,33 @@ def pauli_sum(n: int, terms):
     if not diags:
         diags = {0: np.zeros(N, dtype=np.complex128)}
     return _assemble(n, diags)
+
+
+def pauli_masks(n: int, terms):
+    """(coeffs, x_masks, z_masks) for diaq_matrix_from_pauli from (coeff, {qubit: 'X'|'Y'|'Z'})
+    terms; bit p of a mask belongs to qubit n-1-p."""
+    cs, xs, zs = [], [], []
+    for coeff, ops in terms:
+        x = z = 0
+        for q, p in ops.items():
+            b = 1 << (n - 1 - q)
+            if p in ("X", "Y"):
+                x |= b
+            if p in ("Z", "Y"):
+                z |= b
+        cs.append(complex(coeff))
+        xs.append(x)
+        zs.append(z)
+    return np.array(cs, dtype=np.complex128), np.array(xs, dtype=np.uint64), np.array(zs, dtype=np.uint64)
+
+
+def random_pauli_terms(n: int, rng, n_strings: int, max_weight: int = 3):
+    """n_strings random Pauli strings of weight 1..max_weight on distinct qubits with N(0,1)
+    coefficients -- the training distribution of the learned (s, m) selector."""
+    terms = []
+    for _ in range(n_strings):
+        w = int(rng.integers(1, max_weight + 1))
+        qs = rng.choice(n, size=w, replace=False)
+        ops = {int(q): "XYZ"[int(rng.integers(0, 3))] for q in qs}
+        terms.append((float(rng.standard_normal()), ops))
+    return terms

@@ -49,6 +49,7 @@ typedef enum {
 
 typedef struct diaq_matrix_s *diaq_matrix_t;
 typedef struct diaq_evolve_s *diaq_evolve_t;
+typedef struct diaq_mlp_s *diaq_mlp_t;
 
 /* Message of the last failing call on this thread ("" if none). */
 const char *diaq_last_error(void);
@@ -93,6 +94,16 @@ int diaq_matrix_convert(diaq_matrix_t A, int precision, void *stream, diaq_matri
 /* Drop the diagonals whose values are all exactly zero (real and imaginary == 0.0).  Replaces
  * diaQMatrix::pruneMatrix (src/diaQMatrix.hpp:1543-1604). */
 int diaq_matrix_prune(diaq_matrix_t A, void *stream, diaq_matrix_t *out);
+
+/* H = sum_k c_k P_k built on the device from n_strings Pauli strings over n_qubits (<= 30).
+ * String k: complex coefficient (coeff_re[k], coeff_im[k]; coeff_im may be NULL), flip mask
+ * x_mask[k] (X or Y) and phase mask z_mask[k] (Z or Y) over the basis index, bit p belonging to
+ * qubit n_qubits-1-p (qubit 0 most significant, the Kronecker order).  The result holds the
+ * diagonals that are not exactly zero, ascending.  Replaces building Hamiltonians with the
+ * Kronecker helpers (src/spKron.cpp:189-1271), which overflow 32-bit indices at 2^16 rows. */
+int diaq_matrix_from_pauli(int n_qubits, int32_t n_strings, const double *coeff_re,
+                           const double *coeff_im, const uint64_t *x_mask, const uint64_t *z_mask,
+                           int precision, void *stream, diaq_matrix_t *out);
 
 /* ------------------------------------------------------------------------------------------
  * SpMV.  Replaces spmv_device (src/spMV_gpu.cu:142-168): y = A x on device arrays, y
@@ -222,6 +233,41 @@ int diaq_select_sm_min_cost(double norm1, double tau, double tol, int max_s, int
  * hamiltonian_simulation_cuda does.  Synchronous. */
 int diaq_ham_sim_host(diaq_matrix_t H, const double *psi0_re, const double *psi0_im, double t,
                       int64_t r, int max_iterations, double *psi_re, double *psi_im);
+
+/* ------------------------------------------------------------------------------------------
+ * The learned (s, m) proposer: an FP32 MLP 16 -> 64 -> 64 -> 21 + 30 logits (ReLU), trained
+ * with softmax cross-entropy on both heads (s in 0..20, m in 1..30) and Adam.  No counterpart in
+ * the reference, whose exponential picks s by the norm bound alone (src/spME.cpp:256-262).
+ * All arrays are device arrays, row-major (row b = one instance): X[B][16] float32, labels
+ * int32.  Asynchronous on stream except create/destroy/get/set.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Number of float parameters (W1[16][64] b1[64] W2[64][64] b2[64] W3[64][51] b3[51]). */
+int diaq_mlp_num_params(void);
+
+/* He-initialised network (deterministic for a seed), Adam state zeroed. */
+int diaq_mlp_create(uint64_t seed, diaq_mlp_t *out);
+int diaq_mlp_destroy(diaq_mlp_t M);
+
+/* Copy the flat parameter vector to / from the host (set also resets the Adam state). */
+int diaq_mlp_get_params(diaq_mlp_t M, float *host_out);
+int diaq_mlp_set_params(diaq_mlp_t M, const float *host_in);
+
+/* logits[B][51]: the 21 s-logits then the 30 m-logits. */
+int diaq_mlp_forward(diaq_mlp_t M, const float *X, int B, float *logits, void *stream);
+
+/* Gradient of the mean (over the batch) of CE_s + CE_m into grad_out[num_params] and the
+ * per-row loss into loss_out[B] (either may be NULL); parameters unchanged. */
+int diaq_mlp_gradient(diaq_mlp_t M, const float *X, const int32_t *s_label, const int32_t *m_label,
+                      int B, float *grad_out, float *loss_out, void *stream);
+
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the batch's gradient; loss_out[B] may be NULL. */
+int diaq_mlp_train_step(diaq_mlp_t M, const float *X, const int32_t *s_label,
+                        const int32_t *m_label, int B, float lr, float *loss_out, void *stream);
+
+/* argmax of each head: s_out[B] in 0..20, m_out[B] in 1..30. */
+int diaq_mlp_propose(diaq_mlp_t M, const float *X, int B, int32_t *s_out, int32_t *m_out,
+                     void *stream);
 
 #ifdef __cplusplus
 }
