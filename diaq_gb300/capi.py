@@ -54,6 +54,7 @@ SIGNATURES = {
     "diaq_evolve_launches_per_step": (INT, [P]),
     "diaq_evolve_run_host": (INT, [P, P, P, F64, I64, INT, INT]),
     "diaq_select_sm_min_cost": (INT, [F64, F64, F64, INT, INT, P, P]),
+    "diaq_ham_sim_noalloc": (INT, [P, P, P, F64, I64, INT, P, P, P]),
     "diaq_matrix_from_pauli": (INT, [INT, I32, P, P, P, P, INT, P, P]),
     "diaq_mlp_num_params": (INT, []),
     "diaq_mlp_create": (INT, [ctypes.c_uint64, P]),

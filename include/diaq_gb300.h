@@ -269,6 +269,17 @@ int diaq_mlp_train_step(diaq_mlp_t M, const float *X, const int32_t *s_label,
 int diaq_mlp_propose(diaq_mlp_t M, const float *X, int B, int32_t *s_out, int32_t *m_out,
                      void *stream);
 
+/* diaq_ham_sim for callers that cannot allocate device memory.  No counterpart in the
+ * reference.  Same arguments, results and stream semantics as diaq_ham_sim, but its work
+ * vectors live in a scratch array built into the library (3 MiB per GPU, held until the process
+ * exits) instead of cudaMallocAsync, so the call allocates nothing.  Limit: H may have at most
+ * 65536 rows (16 qubits); larger matrices are rejected with DIAQ_ERR_INVALID.  All calls share
+ * the scratch: calls whose work overlaps on the GPU (other streams, other host threads) race on
+ * it.  The first call on a device looks up the scratch's device address; make that first call
+ * before any stream capture. */
+int diaq_ham_sim_noalloc(diaq_matrix_t H, const double *psi0_re, const double *psi0_im, double t,
+                         int64_t r, int max_iterations, double *psi_re, double *psi_im, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
