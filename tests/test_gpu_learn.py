@@ -1,0 +1,62 @@
+"""The learned (s, m) selection end to end on a small scale: labels meet the tolerance, the
+network trained by the project's kernels proposes, every proposal is checked, and the checked
+choice is never less accurate and never dearer than the norm-bound selection -- and cheaper
+on average, which is the gain the network brings."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_labels_meet_tolerance(native):
+    from diaq_gb300 import learn
+
+    rng = np.random.default_rng(5)
+    for _ in range(12):
+        n, terms, t, tol = learn.random_instance(rng, 8, 10)
+        r = learn.instance_record(n, terms, t, tol, seed=int(rng.integers(1 << 30)))
+        s, m, cost = r["label"]
+        assert learn._error(r["U"], t, s, m, r["norm1"]) <= tol
+        s_ref, m_ref = r["ref"]
+        assert cost <= 2 ** s_ref * m_ref
+        assert r["f"].shape == (16,) and np.all(np.isfinite(r["f"]))
+
+
+def test_chain_tail_matches_evolution(native):
+    """The chain's truncation error equals the error of an actual Taylor step on the GPU."""
+    import torch
+
+    from diaq_gb300 import capi, learn
+    from diaq_gb300 import hamiltonians as ham
+    from oracle import oracle as orc
+
+    rng = np.random.default_rng(8)
+    n, terms, _, _ = learn.random_instance(rng, 9, 9)
+    H = learn.build(n, terms)
+    psi = ham.random_state(1 << n, 3)
+    U = learn.chain(H, torch.from_numpy(psi).cuda())
+    off, re, im = H.download()
+    A = orc.OMatrix(1 << n, 1 << n, off, re, im)
+    exact = orc.ham_sim(A, psi, 0.05, 1, 60)
+    tail, _ = learn.tails(U, 0.05)
+    for m in (3, 6, 10):
+        approx = orc.ham_sim(A, psi, 0.05, 1, m)
+        assert abs(np.linalg.norm(approx - exact) - tail[m - 1]) <= 1e-12 + 1e-6 * tail[m - 1]
+
+
+def test_trained_selector_gains_over_norm_bound(native):
+    from diaq_gb300 import learn
+
+    X, ys, ym, cost_lab, cost_ref = learn.generate(600, seed=2, n_lo=8, n_hi=10, log_every=0)
+    assert np.all(cost_lab <= cost_ref)
+    net, hist = learn.train(X, ys, ym, epochs=60, batch=128, lr=3e-3, log=False)
+    assert hist[-1] < hist[0]
+    rows = learn.evaluate(net, 25, seed=99, n_lo=10, n_hi=11)
+    for r in rows:
+        assert r["cost"] <= r["cost_ref"]
+        if not math.isnan(r["err"]):
+            assert r["err"] <= r["tol"]
+    gain = np.mean([r["cost_ref"] / r["cost"] for r in rows])
+    assert gain > 1.0, gain

@@ -153,3 +153,23 @@ def _rand(rng, r, c):
         idx = np.arange(max(0, -o), min(r, c - o))
         A[idx, idx + o] = rng.standard_normal(len(idx)) + 1j * rng.standard_normal(len(idx))
     return A
+
+
+def test_mlp_oracle_gradient_finite_differences():
+    from oracle import mlp as omlp
+
+    rng = np.random.default_rng(0)
+    p = (rng.standard_normal(omlp.N_PARAMS) * 0.2).astype(np.float32)
+    X = rng.standard_normal((9, 16))
+    ys = rng.integers(0, 21, 9)
+    ym = rng.integers(1, 31, 9)
+    loss, g = omlp.loss_and_grad(p, X, ys, ym)
+    assert loss.shape == (9,) and g.shape == (omlp.N_PARAMS,)
+    pd = p.astype(np.float64)
+    for idx in rng.choice(omlp.N_PARAMS, 12, replace=False):
+        h = 1e-6
+        pp, pm = pd.copy(), pd.copy()
+        pp[idx] += h
+        pm[idx] -= h
+        fd = (omlp.loss_and_grad(pp, X, ys, ym)[0].mean() - omlp.loss_and_grad(pm, X, ys, ym)[0].mean()) / (2 * h)
+        assert abs(fd - g[idx]) <= 1e-7 + 1e-5 * abs(g[idx])
