@@ -264,6 +264,23 @@ def run_spmv_only(args):
     print(json.dumps({"mode": "spmv", "n_qubits": args.n, **out}), flush=True)
 
 
+def chosen_schedule(capi, H, norm1):
+    """(s, m, how) of the chosen form: the trained network's checked proposal when the package
+    ships one, else the cheapest (s, m) under the remainder bound."""
+    from diaq_gb300 import learn
+
+    if os.path.exists(learn.PARAMS_PATH):
+        s, m, src, rec = learn.learned_sm(H, DT, TOL_STEP)
+        del rec
+        import torch
+
+        torch.cuda.empty_cache()
+        if src == "learned":
+            return s, m, "learned (MLP proposal, next-term check)"
+    s, m = capi.select_sm_min_cost(norm1, DT, TOL_STEP, 12, 60)
+    return s, m, "min-cost remainder bound"
+
+
 def run_chosen_only(args):
     """Only the chosen form's evolution, W + K steps (a light command for profilers)."""
     import torch
@@ -277,7 +294,7 @@ def run_chosen_only(args):
     H = capi.Matrix.create(N, N, off, re, im)
     norm1 = ctypes.c_double()
     capi.check(L.diaq_norm1_est(H.h, ctypes.byref(norm1), None))
-    s_c, m_c = capi.select_sm_min_cost(norm1.value, DT, TOL_STEP, 12, 60)
+    s_c, m_c, _ = chosen_schedule(capi, H, norm1.value)
     E = capi.Evolve(H, args.states, capi.EVOLVE_MIXED)
     P0 = ham.random_state(N, 0, k=args.states) if args.states > 1 else ham.random_state(N, 0)[None, :]
     pr = torch.from_numpy(np.ascontiguousarray(P0.real)).cuda()
@@ -320,8 +337,8 @@ def run_ours(args, rank, world):
     ms_plain = _max_over_ranks(_timed(stream, lambda: plain.run(ppr, ppi, N, DT, K, s_p, m_p, sp)), world, dev)
     lps_plain = plain.launches_per_step()
 
-    # ---- chosen form: S states per launch, complex64 terms + FP64 state, cost-optimal (s, m) ----
-    s_c, m_c = capi.select_sm_min_cost(norm1.value, DT, TOL_STEP, 12, 60)
+    # ---- chosen form: S states per launch, complex64 terms + FP64 state, learned (s, m) ----
+    s_c, m_c, selection = chosen_schedule(capi, H, norm1.value)
     chosen = capi.Evolve(H, S, capi.EVOLVE_MIXED)
     P0 = ham.random_state(N, 0, k=S) if S > 1 else p0[None, :]
     cpr = torch.from_numpy(np.ascontiguousarray(P0.real)).to(dev)
@@ -387,7 +404,8 @@ def run_ours(args, rank, world):
         "dtype": "f32 terms + f64 state", "data": "synthetic (seeded XXZ couplings and states, built in-process)",
         "config": {"workload": f"xxz{args.n}_periodic_evolve", "form": "chosen", "n_qubits": args.n, "rows": N,
                    "ndiag": len(off), "stored_values": total, "dt": DT, "states_per_gpu": S,
-                   "substeps": 1 << s_c, "taylor_terms": m_c, "selection": "min-cost remainder bound",
+                   "substeps": 1 << s_c, "taylor_terms": m_c, "selection": selection,
+                   "launch_shape": {"states_per_launch": chosen.config()[0], "rows_per_thread": chosen.config()[1]},
                    "tol_per_step": TOL_STEP, "norm1": norm1.value,
                    "l2": "inputs larger than L2 (c64 matrix 327 MB, states 128 MB > 129 MB)",
                    "parallelism": f"replicas{world}"},

@@ -16,8 +16,15 @@
 // have used):
 //   C128:  psi (caller's), sum, term_a, term_b                 (float64)
 //   MIXED: psi (caller's, float64); v_a, v_b, hi, lo           (float32)
+#include <sys/stat.h>
+
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
 #include <map>
+#include <sstream>
+#include <string>
 #include <tuple>
 
 #include "spmv_kernel.cuh"
@@ -162,6 +169,8 @@ struct EvolvePlan {
     };
     std::map<Key, cudaGraphExec_t> graphs;
     int launches_per_step = 0;
+    SpmvCfg cfg;          // launch shape of the term kernel
+    bool tuned = false;   // cfg chosen (by the autotuner or the caller)
 
     ~EvolvePlan() {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -232,7 +241,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
                 e.outi = oth_i;
                 e.ld = L;
                 e.scale = tau / (double)t;
-                DQ_TRY(launch_dia_spmv_rhs<double>(*P.H, tin_r, tin_i, L, (int)k, e, P.s));
+                DQ_TRY((launch_dia_spmv_rhs_cfg<double, EpiPlain, 2, 1>(*P.H, tin_r, tin_i, L, (int)k, e, P.s, P.cfg)));
                 ++P.launches_per_step;
                 tin_r = tout_r;
                 tin_i = tout_i;
@@ -271,7 +280,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
             e.scale = (float)(tau / (double)t);
             e.first = (t == 1);
             e.last = (t == m);
-            DQ_TRY(launch_dia_spmv_rhs<float>(*P.Hc, in_r, in_i, L, (int)k, e, P.s));
+            DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiMixed, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg)));
             ++P.launches_per_step;
             std::swap(in_r, out_r);
             std::swap(in_i, out_i);
@@ -284,11 +293,158 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
     return DIAQ_OK;
 }
 
+// ---- autotuner ----------------------------------------------------------------------------------------
+// Candidate launch shapes (states per launch, rows per thread) are timed on two steps of the
+// caller's problem, run on scratch copies of the states (the caller's are not advanced), and the
+// fastest is kept.  Choices are cached in a JSON file (DIAQ_AUTOTUNE_CACHE, else
+// $HOME/.cache/diaq_gb300/autotune.json) keyed by GPU, mode, rows, diagonals, states and (s, m).
+
+static std::string cache_path() {
+    if (const char *p = std::getenv("DIAQ_AUTOTUNE_CACHE")) return p;
+    const char *home = std::getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/diaq_gb300/autotune.json";
+}
+
+// The cache is a flat JSON object {"key": [kmax, vr], ...}.
+static std::map<std::string, std::pair<int, int>> read_cache() {
+    std::map<std::string, std::pair<int, int>> out;
+    std::ifstream f(cache_path());
+    if (!f) return out;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string t = ss.str();
+    size_t i = 0;
+    while ((i = t.find('"', i)) != std::string::npos) {
+        const size_t j = t.find('"', i + 1);
+        if (j == std::string::npos) break;
+        const std::string key = t.substr(i + 1, j - i - 1);
+        int a = 0, b = 0;
+        const size_t br = t.find('[', j);
+        if (br == std::string::npos || std::sscanf(t.c_str() + br, "[%d ,%d]", &a, &b) != 2) break;
+        out[key] = {a, b};
+        i = t.find(']', br);
+        if (i == std::string::npos) break;
+    }
+    return out;
+}
+
+static void write_cache(const std::map<std::string, std::pair<int, int>> &c) {
+    const std::string path = cache_path();
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {
+        // create the directory (one level below an existing parent is all we need)
+        std::string dir = path.substr(0, slash);
+        for (size_t k = 1; k <= dir.size(); ++k)
+            if (k == dir.size() || dir[k] == '/') mkdir(dir.substr(0, k).c_str(), 0755);
+    }
+    std::ofstream f(path + ".tmp");
+    if (!f) return;
+    f << "{\n";
+    size_t n = 0;
+    for (const auto &kv : c) f << "  \"" << kv.first << "\": [" << kv.second.first << ", " << kv.second.second << "]" << (++n < c.size() ? ",\n" : "\n");
+    f << "}\n";
+    f.close();
+    std::rename((path + ".tmp").c_str(), path.c_str());
+}
+
+static std::string tune_key(const EvolvePlan &P, int sl, int m) {
+    cudaDeviceProp prop{};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaGetDeviceProperties(&prop, dev);
+    std::string name(prop.name);
+    for (auto &ch : name)
+        if (ch == '"' || ch == ' ') ch = '_';
+    char buf[256];
+    std::snprintf(buf, sizeof(buf), "%s|%s|n=%lld|nd=%d|k=%d|s=%d|m=%d", name.c_str(),
+                  P.mode == DIAQ_EVOLVE_MIXED ? "mixed" : "c128", (long long)P.n, P.H->nd, P.nrhs, sl, m);
+    return buf;
+}
+
+static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double *pi, int64_t ld, cudaStream_t user) {
+    std::vector<SpmvCfg> cand;
+    if (P.mode == DIAQ_EVOLVE_MIXED)
+        cand = {{8, 1}, {8, 2}, {8, 4}, {4, 2}, {4, 4}, {2, 4}, {1, 4}};
+    else
+        cand = {{8, 1}, {8, 2}, {4, 2}, {2, 2}, {1, 2}};
+    // drop shapes with more states per launch than the plan has (same launches as a smaller one)
+    int kcap = 1;
+    while (kcap < P.nrhs && kcap < 8) kcap *= 2;
+    std::vector<SpmvCfg> c2;
+    for (auto c : cand)
+        if (c.kmax <= kcap) c2.push_back(c);
+    cand.swap(c2);
+    const std::string key = tune_key(P, sl, m);
+    auto cache = read_cache();
+    auto hit = cache.find(key);
+    if (hit != cache.end()) {
+        P.cfg = SpmvCfg{hit->second.first, hit->second.second};
+        P.tuned = true;
+        return DIAQ_OK;
+    }
+    if (cand.size() == 1) {
+        P.cfg = cand[0];
+        P.tuned = true;
+        return DIAQ_OK;
+    }
+    // scratch copies of the states
+    const size_t cnt = (size_t)P.nrhs * (size_t)P.n;
+    double *tmp = nullptr;
+    DQ_CUDA(cudaMalloc(&tmp, 2 * cnt * sizeof(double)));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int st = DIAQ_OK;
+    float best = -1.f;
+    SpmvCfg best_cfg = cand[0];
+    cudaError_t e = cudaStreamSynchronize(user);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(tmp, pr, cnt * sizeof(double), cudaMemcpyDeviceToDevice, P.s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(tmp + cnt, pi, cnt * sizeof(double), cudaMemcpyDeviceToDevice, P.s);
+    if (e != cudaSuccess) st = cuda_status(e, "autotune", __FILE__, __LINE__);
+    for (size_t c = 0; c < cand.size() && st == DIAQ_OK; ++c) {
+        P.cfg = cand[c];
+        if (P.mode == DIAQ_EVOLVE_MIXED) {
+            float *var = (float *)P.buf, *vai = var + cnt;
+            const int grid = (int)std::min<int64_t>(((int64_t)cnt + 255) / 256, 8 * num_sms());
+            to_f32_kernel<<<grid, 256, 0, P.s>>>(tmp, var, (int64_t)cnt);
+            to_f32_kernel<<<grid, 256, 0, P.s>>>(tmp + cnt, vai, (int64_t)cnt);
+        }
+        st = enqueue_step(P, dt, sl, m, tmp, tmp + cnt, P.n);  // warm-up
+        if (st != DIAQ_OK) break;
+        cudaEventRecord(e0, P.s);
+        st = enqueue_step(P, dt, sl, m, tmp, tmp + cnt, P.n);
+        if (st != DIAQ_OK) break;
+        cudaEventRecord(e1, P.s);
+        e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            st = cuda_status(e, "autotune", __FILE__, __LINE__);
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (best < 0.f || ms < best) {
+            best = ms;
+            best_cfg = cand[c];
+        }
+    }
+    cudaStreamSynchronize(P.s);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(tmp);
+    if (st != DIAQ_OK) return st;
+    P.cfg = best_cfg;
+    P.tuned = true;
+    cache[key] = {best_cfg.kmax, best_cfg.vr};
+    write_cache(cache);
+    return DIAQ_OK;
+}
+
 static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt, int64_t steps, int sl, int m,
                     cudaStream_t user) {
     if (steps < 0 || m < 0 || sl < 0 || sl > 20) return set_error(DIAQ_ERR_INVALID, "evolve: bad steps / s / m");
     if (!pr || !pi) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
     if (steps == 0 || m == 0 || P.n == 0) return DIAQ_OK;
+    if (!P.tuned) DQ_TRY(autotune(P, dt, sl, m, pr, pi, ld, user));
     const EvolvePlan::Key key{dt, sl, m, pr, pi, ld};
     auto it = P.graphs.find(key);
     if (it == P.graphs.end()) {
@@ -348,6 +504,31 @@ int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld,
 }
 
 int diaq_evolve_launches_per_step(diaq_evolve_t E) { return E ? E->launches_per_step : 0; }
+
+int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread) {
+    if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
+    if (states_per_launch == 0) {  // back to automatic choice
+        E->tuned = false;
+        E->cfg = SpmvCfg{};
+    } else {
+        const bool f32 = E->mode == DIAQ_EVOLVE_MIXED;
+        const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
+        if (states_per_launch < 1 || states_per_launch > 8 || !vr_ok)
+            return set_error(DIAQ_ERR_INVALID, "evolve: states_per_launch in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
+        E->cfg = SpmvCfg{states_per_launch, rows_per_thread};
+        E->tuned = true;
+    }
+    for (auto &kv : E->graphs) cudaGraphExecDestroy(kv.second);
+    E->graphs.clear();
+    return DIAQ_OK;
+}
+
+int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread) {
+    if (!E || !states_per_launch || !rows_per_thread) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    *states_per_launch = E->cfg.kmax;
+    *rows_per_thread = E->cfg.vr > 0 ? E->cfg.vr : (E->mode == DIAQ_EVOLVE_MIXED ? 4 : 2);
+    return DIAQ_OK;
+}
 
 int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
                          int substeps_log2, int m) {

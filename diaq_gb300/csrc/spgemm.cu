@@ -191,14 +191,14 @@ __global__ void __launch_bounds__(kSpmvThreads)
                 const int64_t hi = min(min(ma.hi, mb.hi - (int64_t)ma.off), mc.hi);
                 if (r0 + V <= lo || r0 >= hi) continue;
                 T ar[V], ai[V], br[V], bi[V];
-                load_vec<T>(ar, Are + ma.base + r0);
-                load_vec<T>(ai, Aim + ma.base + r0);
+                load_vec<T, V>(ar, Are + ma.base + r0);
+                load_vec<T, V>(ai, Aim + ma.base + r0);
                 const bool full = (r0 >= lo) && (r0 + V <= hi);
                 const T *pbr = Bre + mb.base + r0 + ma.off;
                 const T *pbi = Bim + mb.base + r0 + ma.off;
                 if (full && aligned16(pbr)) {
-                    load_vec<T>(br, pbr);
-                    load_vec<T>(bi, pbi);
+                    load_vec<T, V>(br, pbr);
+                    load_vec<T, V>(bi, pbi);
                 } else {
 #pragma unroll
                     for (int v = 0; v < V; ++v) {

@@ -20,24 +20,42 @@ namespace diaq_gb300 {
 constexpr int kSpmvThreads = 256;
 constexpr int kMetaChunk = 256;
 
-template <typename T>
-struct VecOf;
+// VR consecutive values of T as one aligned vector load (VR * sizeof(T) bytes).
+template <typename T, int VR>
+struct Vec;
 template <>
-struct VecOf<double> {
+struct Vec<double, 2> {
     using type = double2;
-    static constexpr int V = 2;
 };
 template <>
-struct VecOf<float> {
+struct Vec<double, 1> {
+    using type = double;
+};
+template <>
+struct Vec<float, 4> {
     using type = float4;
-    static constexpr int V = 4;
+};
+template <>
+struct Vec<float, 2> {
+    using type = float2;
+};
+template <>
+struct Vec<float, 1> {
+    using type = float;
 };
 
+// The widest vector: 16 bytes.
 template <typename T>
-__device__ __forceinline__ void load_vec(T (&dst)[VecOf<T>::V], const T *p) {
-    using VT = typename VecOf<T>::type;
-    const VT v = __ldg(reinterpret_cast<const VT *>(p));
-    if constexpr (VecOf<T>::V == 2) {
+struct VecOf {
+    static constexpr int V = 16 / sizeof(T);
+    using type = typename Vec<T, V>::type;
+};
+
+template <typename VT, typename T, int VR>
+__device__ __forceinline__ void unpack(T (&dst)[VR], const VT &v) {
+    if constexpr (VR == 1) {
+        dst[0] = v;
+    } else if constexpr (VR == 2) {
         dst[0] = v.x;
         dst[1] = v.y;
     } else {
@@ -46,34 +64,35 @@ __device__ __forceinline__ void load_vec(T (&dst)[VecOf<T>::V], const T *p) {
         dst[2] = v.z;
         dst[3] = v.w;
     }
+}
+
+template <typename T, int VR = VecOf<T>::V>
+__device__ __forceinline__ void load_vec(T (&dst)[VR], const T *p) {
+    using VT = typename Vec<T, VR>::type;
+    unpack<VT, T, VR>(dst, __ldg(reinterpret_cast<const VT *>(p)));
 }
 
 // Matrix values stream once: evict them first from L2, keeping x resident.
-template <typename T>
-__device__ __forceinline__ void load_vec_stream(T (&dst)[VecOf<T>::V], const T *p) {
-    using VT = typename VecOf<T>::type;
-    const VT v = __ldcs(reinterpret_cast<const VT *>(p));
-    if constexpr (VecOf<T>::V == 2) {
-        dst[0] = v.x;
-        dst[1] = v.y;
-    } else {
-        dst[0] = v.x;
-        dst[1] = v.y;
-        dst[2] = v.z;
-        dst[3] = v.w;
-    }
+template <typename T, int VR = VecOf<T>::V>
+__device__ __forceinline__ void load_vec_stream(T (&dst)[VR], const T *p) {
+    using VT = typename Vec<T, VR>::type;
+    unpack<VT, T, VR>(dst, __ldcs(reinterpret_cast<const VT *>(p)));
 }
 
-__device__ __forceinline__ bool aligned16(const void *p) {
-    return (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+template <int BYTES>
+__device__ __forceinline__ bool aligned_to(const void *p) {
+    return (reinterpret_cast<uintptr_t>(p) & (uintptr_t)(BYTES - 1)) == 0;
 }
+__device__ __forceinline__ bool aligned16(const void *p) { return aligned_to<16>(p); }
 
-template <typename T, int K, class Epi>
+// K states (kq of them live), VR rows per thread.
+template <typename T, int K, int VR, class Epi>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_kernel(const DiagMeta *__restrict__ meta, int nd, const T *__restrict__ are,
                     const T *__restrict__ aim, int64_t rows, const T *__restrict__ xr,
                     const T *__restrict__ xi, int64_t ldx, int kq, Epi epi) {
-    constexpr int V = VecOf<T>::V;
+    constexpr int V = VR;
+    constexpr int VB = VR * (int)sizeof(T);
     __shared__ DiagMeta sm[kMetaChunk];
     const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
     T accr[K][V], acci[K][V];
@@ -95,8 +114,8 @@ __global__ void __launch_bounds__(kSpmvThreads)
             const int64_t base = sm[k].base;
             const int64_t d = sm[k].off;
             T ar[V], ai[V];
-            load_vec_stream<T>(ar, are + base + r0);
-            load_vec_stream<T>(ai, aim + base + r0);
+            load_vec_stream<T, V>(ar, are + base + r0);
+            load_vec_stream<T, V>(ai, aim + base + r0);
             const bool full = (r0 >= lo) && (r0 + V <= hi);
             if (!full) {
 #pragma unroll
@@ -110,9 +129,9 @@ __global__ void __launch_bounds__(kSpmvThreads)
                 const T *pxr = xr + q * ldx + c;
                 const T *pxi = xi + q * ldx + c;
                 T xrv[V], xiv[V];
-                if (full && aligned16(pxr) && aligned16(pxi)) {
-                    load_vec<T>(xrv, pxr);
-                    load_vec<T>(xiv, pxi);
+                if (full && aligned_to<VB>(pxr) && aligned_to<VB>(pxi)) {
+                    load_vec<T, V>(xrv, pxr);
+                    load_vec<T, V>(xiv, pxi);
                 } else {
 #pragma unroll
                     for (int v = 0; v < V; ++v) {
@@ -145,18 +164,20 @@ struct EpiStore {
         for (int q = 0; q < K; ++q) {
             if (q >= kq) break;
             T *pr = yr + q * ldy + r0, *pi = yi + q * ldy + r0;
-            if (r0 + V <= rows && aligned16(pr) && aligned16(pi)) {
-                using VT = typename VecOf<T>::type;
+            if (V > 1 && r0 + V <= rows && aligned_to<V * sizeof(T)>(pr) && aligned_to<V * sizeof(T)>(pi)) {
+                using VT = typename Vec<T, V>::type;
                 VT a, b;
                 if constexpr (V == 2) {
                     a = VT{ar[q][0], ar[q][1]};
                     b = VT{ai[q][0], ai[q][1]};
-                } else {
+                } else if constexpr (V == 4) {
                     a = VT{ar[q][0], ar[q][1], ar[q][2], ar[q][3]};
                     b = VT{ai[q][0], ai[q][1], ai[q][2], ai[q][3]};
                 }
-                *reinterpret_cast<VT *>(pr) = a;
-                *reinterpret_cast<VT *>(pi) = b;
+                if constexpr (V > 1) {
+                    *reinterpret_cast<VT *>(pr) = a;
+                    *reinterpret_cast<VT *>(pi) = b;
+                }
             } else {
 #pragma unroll
                 for (int v = 0; v < V; ++v)
@@ -210,37 +231,62 @@ inline unsigned spmv_blocks(int64_t rows, int V) {
     return (unsigned)((rows + per - 1) / per);
 }
 
-// Launch over the right-hand sides in chunks of up to 8 (one matrix read per chunk, the kernel
-// instantiated for 1, 2, 4 or 8 with the unused slots masked); Epi must offer `shifted(q0)`, the
-// same epilogue for right-hand sides q0.. .
-template <typename T, class Epi>
-int launch_dia_spmv_rhs(const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, Epi epi,
-                        cudaStream_t s) {
-    constexpr int V = VecOf<T>::V;
+// Launch shape of the SpMV family: at most kmax states per launch (the matrix is read once per
+// launch), vr rows per thread (the tile of a block is 256 * vr rows).  vr = 0 picks the widest
+// 16-byte vector.
+struct SpmvCfg {
+    int kmax = 8;
+    int vr = 0;
+};
+
+template <typename T, int K, class Epi, int VR, int... More>
+void launch_vr(int vr, const Matrix &A, const T *xr, const T *xi, int64_t ldx, int kq, const Epi &e,
+               cudaStream_t s) {
+    if constexpr (sizeof...(More) > 0) {
+        if (vr != VR) {
+            launch_vr<T, K, Epi, More...>(vr, A, xr, xi, ldx, kq, e, s);
+            return;
+        }
+    }
+    dia_spmv_kernel<T, K, VR, Epi><<<spmv_blocks(A.rows, VR), kSpmvThreads, 0, s>>>(
+        A.d_meta, A.nd, (const T *)A.re, (const T *)A.im, A.rows, xr, xi, ldx, kq, e);
+}
+
+// Launch over the right-hand sides in chunks of up to cfg.kmax (<= 8; one matrix read per chunk,
+// the kernel instantiated for 1, 2, 4 or 8 states with the unused slots masked).  VRs lists the
+// rows-per-thread variants compiled for this epilogue (the first is the default).  Epi must
+// offer `shifted(q0)`, the same epilogue for right-hand sides q0.. .
+template <typename T, class Epi, int... VRs>
+int launch_dia_spmv_rhs_cfg(const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, Epi epi,
+                            cudaStream_t s, SpmvCfg cfg) {
     if (A.rows == 0 || nrhs <= 0) return DIAQ_OK;
-    const unsigned grid = spmv_blocks(A.rows, V);
+    const int kmax = cfg.kmax >= 8 ? 8 : cfg.kmax >= 4 ? 4 : cfg.kmax >= 2 ? 2 : 1;
+    const int vr = cfg.vr > 0 ? cfg.vr : VecOf<T>::V;
     int q0 = 0;
     while (q0 < nrhs) {
         const int left = nrhs - q0;
-        const int kq = left < 8 ? left : 8;  // states in this launch; the matrix is read once for them
+        const int kq = left < kmax ? left : kmax;
         const T *pxr = xr + q0 * ldx, *pxi = xi + q0 * ldx;
         const Epi e = epi.shifted(q0);
         if (kq > 4)
-            dia_spmv_kernel<T, 8, Epi><<<grid, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const T *)A.re, (const T *)A.im,
-                                                                     A.rows, pxr, pxi, ldx, kq, e);
+            launch_vr<T, 8, Epi, VRs...>(vr, A, pxr, pxi, ldx, kq, e, s);
         else if (kq > 2)
-            dia_spmv_kernel<T, 4, Epi><<<grid, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const T *)A.re, (const T *)A.im,
-                                                                     A.rows, pxr, pxi, ldx, kq, e);
+            launch_vr<T, 4, Epi, VRs...>(vr, A, pxr, pxi, ldx, kq, e, s);
         else if (kq == 2)
-            dia_spmv_kernel<T, 2, Epi><<<grid, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const T *)A.re, (const T *)A.im,
-                                                                     A.rows, pxr, pxi, ldx, kq, e);
+            launch_vr<T, 2, Epi, VRs...>(vr, A, pxr, pxi, ldx, kq, e, s);
         else
-            dia_spmv_kernel<T, 1, Epi><<<grid, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const T *)A.re, (const T *)A.im,
-                                                                     A.rows, pxr, pxi, ldx, kq, e);
+            launch_vr<T, 1, Epi, VRs...>(vr, A, pxr, pxi, ldx, kq, e, s);
         q0 += kq;
     }
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;
+}
+
+// The default shape: 8 states per launch, 16-byte rows per thread.
+template <typename T, class Epi>
+int launch_dia_spmv_rhs(const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, Epi epi,
+                        cudaStream_t s) {
+    return launch_dia_spmv_rhs_cfg<T, Epi, VecOf<T>::V>(A, xr, xi, ldx, nrhs, epi, s, SpmvCfg{});
 }
 
 template <typename T>

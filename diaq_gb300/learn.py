@@ -170,9 +170,13 @@ def check(U, t, tol, norm1, s, m):
 
 def instance_record(n, terms, t, tol, seed):
     """Everything the selector needs about one instance: features, label, norm-bound choice."""
+    return record_for(build(n, terms), n, t, tol, seed)
+
+
+def record_for(H: capi.Matrix, n, t, tol, seed, with_label=True):
+    """Features, chain, norm-bound choice (and label) for a device matrix H of 2^n rows."""
     import torch
 
-    H = build(n, terms)
     norm1 = ctypes.c_double()
     fro = ctypes.c_double()
     capi.check(capi.lib().diaq_norm1_est(H.h, ctypes.byref(norm1), None))
@@ -181,7 +185,7 @@ def instance_record(n, terms, t, tol, seed):
     psi = torch.from_numpy(ham.random_state(N, seed)).cuda()
     U = chain(H, psi)
     f = features(n, H, U, t, tol, norm1.value, fro.value)
-    lab = label(U, t, tol, norm1.value)
+    lab = label(U, t, tol, norm1.value) if with_label else None
     return {"f": f, "label": lab, "norm1": norm1.value, "U": U, "H": H, "ref": norm_bound(norm1.value, t, tol)}
 
 
@@ -257,14 +261,31 @@ def load(path: str = PARAMS_PATH):
 
 
 def choose(net, record, t, tol):
-    """(s, m, source) for one instance: the network's proposal if it passes the check and costs
-    no more than the norm-bound choice, else the norm-bound choice."""
+    """(s, m, source) for one instance.  The network proposes (s, m); the next-term check then
+    settles the degree near it -- the smallest m' in [m-3, m+4] that passes -- and the result
+    is used when it costs no more than the norm-bound choice, which is taken otherwise."""
     s, m = propose(net, record["f"][None, :])
     s, m = int(s[0]), int(m[0])
     s_ref, m_ref = record["ref"]
-    if 2 ** s * m <= 2 ** s_ref * m_ref and check(record["U"], t, tol, record["norm1"], s, m):
-        return s, m, "learned"
+    for mm in range(max(1, m - 3), min(M_MAX, m + 4) + 1):
+        if 2 ** s * mm > 2 ** s_ref * m_ref:
+            break
+        if check(record["U"], t, tol, record["norm1"], s, mm):
+            return s, mm, "learned"
     return s_ref, m_ref, "norm-bound"
+
+
+def learned_sm(H: capi.Matrix, t: float, tol: float, net=None, seed: int = 12345):
+    """(s, m, source, record) for evolving states under the device matrix H over time t to
+    tolerance tol: the shipped network's checked proposal, or the norm-bound choice."""
+    n = int(H.info()[0]).bit_length() - 1
+    rec = record_for(H, n, t, tol, seed, with_label=False)
+    net = net if net is not None else load()
+    if net is None:
+        s, m = rec["ref"]
+        return s, m, "norm-bound (no trained network)", rec
+    s, m, src = choose(net, rec, t, tol)
+    return s, m, src, rec
 
 
 def evaluate(net, count, seed, n_lo=18, n_hi=20):

@@ -214,6 +214,14 @@ int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld,
 int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
                          int substeps_log2, int m);
 
+/* Launch shape of the plan's term kernel: states per launch (1..8; the matrix is read once per
+ * launch) and rows per thread (1, 2, or 4 for the mixed mode).  0 states = choose automatically:
+ * on the first run the autotuner times the candidate shapes on two steps of scratch copies of
+ * the states and keeps the fastest, caching the choice in a JSON file (DIAQ_AUTOTUNE_CACHE, else
+ * $HOME/.cache/diaq_gb300/autotune.json).  Setting a shape drops the recorded graphs. */
+int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread);
+int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread);
+
 /* Kernel launches in one recorded time step of the last graph built (0 before any run). */
 int diaq_evolve_launches_per_step(diaq_evolve_t E);
 

@@ -38,7 +38,8 @@ def test_plain_matches_oracle(native, sl, m):
     for q in range(3):
         want = orc.ham_sim(A, P[q], 0.05 * 4, 4, m, substeps=1 << sl)
         assert maxrel(got[q], want) < 1e-12, q
-    assert E.launches_per_step() == (1 << sl) * m * 1   # 3 states share each launch
+    k, _ = E.config()
+    assert E.launches_per_step() == (1 << sl) * m * -(-3 // k)   # states share launches, k per launch
 
 
 def test_plain_single_state_equals_reference_rule(native):
@@ -100,3 +101,51 @@ def test_plan_rejects_bad_input(native):
     S = capi.Matrix.create(4, 4, [0], np.ones(4), np.zeros(4), precision=capi.C64)
     with pytest.raises(capi.DiaqError, match="c128"):
         capi.Evolve(S, 1)
+
+
+@pytest.mark.parametrize("cfg", [(8, 1), (8, 2), (8, 4), (4, 2), (4, 4), (2, 4), (1, 4), (1, 1)])
+def test_mixed_every_launch_shape(native, cfg):
+    """Each (states per launch, rows per thread) shape the autotuner may pick gives the same
+    answer (odd sizes: 3 states, 2^11 + rows from a rectangular-free square chain)."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 11, 3, capi.EVOLVE_MIXED)
+    E.set_config(*cfg)
+    assert E.config() == cfg
+    E.run(pr, pi, A.rows, 0.05, 5, 0, 13)
+    got = _result(pr, pi)
+    for q in range(3):
+        want = orc.ham_sim(A, P[q], 0.25, 5, 13)
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
+
+
+@pytest.mark.parametrize("cfg", [(8, 1), (8, 2), (4, 2), (2, 2), (1, 2), (1, 1)])
+def test_plain_every_launch_shape(native, cfg):
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 10, 5, capi.EVOLVE_C128)
+    E.set_config(*cfg)
+    E.run(pr, pi, A.rows, 0.05, 3, 1, 9)
+    got = _result(pr, pi)
+    for q in (0, 4):
+        assert maxrel(got[q], orc.ham_sim(A, P[q], 0.15, 3, 9, substeps=2)) < 1e-12
+
+
+def test_autotuner_caches_its_choice(native, tmp_path, monkeypatch):
+    capi, _ = native
+    cache = tmp_path / "autotune.json"
+    monkeypatch.setenv("DIAQ_AUTOTUNE_CACHE", str(cache))
+    A, E, P, pr, pi = _setup(capi, 12, 4, capi.EVOLVE_MIXED)
+    E.run(pr, pi, A.rows, 0.05, 2, 0, 12)
+    k, v = E.config()
+    assert k in (1, 2, 4) and v in (1, 2, 4)
+    import json
+
+    saved = json.load(open(cache))
+    assert any(val == [k, v] for val in saved.values())
+    # the tuning ran on scratch copies: the states advanced exactly 2 steps
+    got = _result(pr, pi)
+    want = orc.ham_sim(A, P[2], 0.1, 2, 12)
+    assert np.linalg.norm(got[2] - want) / np.linalg.norm(want) < 1e-6
+    # a new plan for the same problem takes the cached shape without timing
+    E2 = capi.Evolve(capi.Matrix.create(A.rows, A.cols, A.off, A.re, A.im), 4, capi.EVOLVE_MIXED)
+    E2.run(pr, pi, A.rows, 0.05, 1, 0, 12)
+    assert E2.config() == (k, v)
