@@ -307,6 +307,163 @@ def run_chosen_only(args):
           flush=True)
 
 
+def _pauli_chain(model, n, rng):
+    """TFIM (open; J ~ U[0.5,1.5], h ~ U[0.2,2]) or XXZ (periodic; J ~ U[0.5,1.5], Delta 0.8,
+    h ~ U[-1,1]) as Pauli strings."""
+    terms = []
+    if model == "tfim":
+        J = rng.uniform(0.5, 1.5, n - 1)
+        h = rng.uniform(0.2, 2.0, n)
+        terms += [(-J[i], {i: "Z", i + 1: "Z"}) for i in range(n - 1)]
+        terms += [(-h[i], {i: "X"}) for i in range(n)]
+    else:
+        J = rng.uniform(0.5, 1.5, n)
+        h = rng.uniform(-1.0, 1.0, n)
+        for i in range(n):
+            j = (i + 1) % n
+            terms += [(J[i], {i: "X", j: "X"}), (J[i], {i: "Y", j: "Y"}), (0.8 * J[i], {i: "Z", j: "Z"})]
+        terms += [(h[i], {i: "Z"}) for i in range(n)]
+    return terms
+
+
+def run_batched(args):
+    """Config 4: many Hamiltonians of uneven size with several states each, one persistent
+    work-queued launch per Taylor phase over all of them, the step recorded as a CUDA graph."""
+    import torch
+
+    from diaq_gb300 import build, capi
+    from diaq_gb300 import hamiltonians as ham
+    from oracle import oracle as orc
+
+    build.build()
+    L = capi.lib()
+    rng = np.random.default_rng(args.batch_seed)
+    specs = []
+    for i in range(args.instances):
+        n = int(rng.integers(args.n_lo, args.n_hi + 1))
+        model = "tfim" if i % 2 == 0 else "xxz"
+        k = int(rng.choice([1, 4, 16]))
+        specs.append((model, n, k, _pauli_chain(model, n, rng)))
+    dt, tol = 0.02, TOL_STEP
+    out = {"mode": "batched", "instances": len(specs), "n_range": [args.n_lo, args.n_hi], "dt": dt,
+           "states": int(sum(k for _, _, k, _ in specs)), "variants": {}}
+    for variant in (["c64", "c128"] if args.variant == "both" else [args.variant]):
+        prec = capi.C64 if variant == "c64" else capi.C128
+        w = 8 if variant == "c64" else 16
+        steps = args.batch_steps if variant == "c64" else args.batch_steps_c128
+        # memory per instance: matrix + states (f64) + 8 work vectors
+        groups, cur, cur_bytes = [], [], 0
+        for idx, (model, n, k, terms) in enumerate(specs):
+            N = 1 << n
+            est = w * (2 * n + 1) * N + 16 * k * N + 8 * w * k * N
+            if cur and cur_bytes + est > args.mem_gb * 1e9:
+                groups.append(cur)
+                cur, cur_bytes = [], 0
+            cur.append(idx)
+            cur_bytes += est
+        groups.append(cur)
+        total_ms, total_states_steps, checks = 0.0, 0, []
+        gen = torch.Generator(device="cuda").manual_seed(7)
+        for grp in groups:
+            mats, prs, pis, sched_s, sched_m = [], [], [], [], []
+            for idx in grp:
+                model, n, k, terms = specs[idx]
+                M = capi.Matrix.from_pauli(n, *ham.pauli_masks(n, terms), precision=prec)
+                nrm = ctypes.c_double()
+                capi.check(L.diaq_norm1_est(M.h, ctypes.byref(nrm), None))
+                s_i, m_i = capi.select_sm_min_cost(nrm.value, dt, tol, 12, 60)
+                z = torch.randn((k, 1 << n), dtype=torch.complex128, device="cuda", generator=gen)
+                z = z / torch.linalg.vector_norm(z, dim=1, keepdim=True)
+                mats.append(M)
+                prs.append(z.real.contiguous())
+                pis.append(z.imag.contiguous())
+                sched_s.append(s_i)
+                sched_m.append(m_i)
+            small = [j for j, idx in enumerate(grp) if specs[idx][1] <= 12][:3]
+            start = {j: (prs[j][0].cpu().numpy() + 1j * pis[j][0].cpu().numpy()) for j in small}
+            B = capi.Batch(mats, prs, pis)
+            stream = torch.cuda.current_stream()
+            B.run(dt, sched_s, sched_m, args.warmup, stream.cuda_stream)
+            torch.cuda.synchronize()
+            ms = _timed(stream, lambda: B.run(dt, sched_s, sched_m, steps, stream.cuda_stream))
+            total_ms += ms
+            total_states_steps += steps * sum(specs[idx][2] for idx in grp)
+            # accuracy on a few small instances: the oracle with the same (s, m), same steps
+            for j in small:
+                idx = grp[j]
+                model, n, k, terms = specs[idx]
+                N2, off, re, im = ham.pauli_sum(n, terms)
+                A = orc.OMatrix(N2, N2, off, re, im)
+                want = orc.ham_sim(A, start[j], dt * (args.warmup + steps), args.warmup + steps, sched_m[j],
+                                   substeps=1 << sched_s[j])
+                got = prs[j][0].cpu().numpy() + 1j * pis[j][0].cpu().numpy()
+                checks.append(float(np.linalg.norm(got - want) / np.linalg.norm(want)))
+            cfg = B.config()
+            del B, mats, prs, pis
+            torch.cuda.empty_cache()
+        out["variants"][variant] = {"value": total_states_steps / (total_ms / 1e3), "unit": "states·steps/s",
+                                    "steps": steps, "groups": len(groups), "ms": total_ms,
+                                    "launch_shape": {"states_per_launch": cfg[0], "rows_per_thread": cfg[1],
+                                                     "phases_per_step_last_group": cfg[2]},
+                                    "rel_err_vs_oracle_max": max(checks) if checks else None,
+                                    "checked_instances": len(checks)}
+    print(json.dumps(out), flush=True)
+
+
+def run_precision(args):
+    """Config 3: the XXZ chain at n qubits (24 by default) evolved to t = 1 in 20 steps in the
+    mixed form, against a complex128 evolution of the same states at a 1e-14 step tolerance."""
+    import torch
+
+    from diaq_gb300 import build, capi
+    from diaq_gb300 import hamiltonians as ham
+
+    build.build()
+    L = capi.lib()
+    n = args.n
+    J, h = ham.xxz_params(n, 1)
+    terms = []
+    for i in range(n):
+        j = (i + 1) % n
+        terms += [(J[i], {i: "X", j: "X"}), (J[i], {i: "Y", j: "Y"}), (0.8 * J[i], {i: "Z", j: "Z"})]
+    terms += [(h[i], {i: "Z"}) for i in range(n)]
+    H = capi.Matrix.from_pauli(n, *ham.pauli_masks(n, terms))
+    N, _, nd, total, _ = H.info()
+    nrm = ctypes.c_double()
+    capi.check(L.diaq_norm1_est(H.h, ctypes.byref(nrm), None))
+    steps, dt, S = 20, 1.0 / 20, args.states
+    s_c, m_c, selection = chosen_schedule(capi, H, nrm.value)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    z = torch.randn((S, N), dtype=torch.complex128, device="cuda", generator=gen)
+    z = z / torch.linalg.vector_norm(z, dim=1, keepdim=True)
+    stream = torch.cuda.current_stream()
+    # mixed
+    pr, pi = z.real.contiguous(), z.imag.contiguous()
+    E = capi.Evolve(H, S, capi.EVOLVE_MIXED)
+    ms_mixed = _timed(stream, lambda: E.run(pr, pi, N, dt, steps, s_c, m_c, stream.cuda_stream))
+    cfg = E.config()
+    del E
+    torch.cuda.empty_cache()
+    # complex128 reference
+    s_r, m_r = capi.select_sm(nrm.value, dt, 1e-14, 1.0, 100)
+    rr, ri = z.real.contiguous(), z.imag.contiguous()
+    R = capi.Evolve(H, S, capi.EVOLVE_C128)
+    ms_ref = _timed(stream, lambda: R.run(rr, ri, N, dt, steps, s_r, m_r, stream.cuda_stream))
+    got, want = pr + 1j * pi, rr + 1j * ri
+    err = (torch.linalg.vector_norm(got - want, dim=1) / torch.linalg.vector_norm(want, dim=1)).cpu().numpy()
+    fid = (torch.abs((want.conj() * got).sum(dim=1)) ** 2 /
+           (torch.linalg.vector_norm(got, dim=1) ** 2 * torch.linalg.vector_norm(want, dim=1) ** 2)).cpu().numpy()
+    drift = (torch.linalg.vector_norm(got, dim=1) - 1).abs().cpu().numpy()
+    print(json.dumps({"mode": "precision", "n_qubits": n, "rows": N, "ndiag": nd, "stored_values": total,
+                      "t": 1.0, "steps": steps, "states": S, "substeps": 1 << s_c, "taylor_terms": m_c,
+                      "selection": selection, "launch_shape": cfg,
+                      "mixed": {"states_steps_per_s": S * steps / (ms_mixed / 1e3), "ms": ms_mixed},
+                      "c128_reference": {"states_steps_per_s": S * steps / (ms_ref / 1e3), "ms": ms_ref,
+                                         "substeps": 1 << s_r, "taylor_terms": m_r},
+                      "rel_err_max": float(err.max()), "fidelity_min": float(fid.min()),
+                      "norm_drift_max": float(drift.max())}), flush=True)
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -440,7 +597,15 @@ def main():
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--spmv-reps", type=int, default=1000)
     ap.add_argument("--states", type=int, default=8, help="states evolved together by the chosen form")
-    ap.add_argument("--mode", choices=["evolve", "spmv", "chosen"], default="evolve",
+    ap.add_argument("--instances", type=int, default=512, help="batched mode: Hamiltonians")
+    ap.add_argument("--n-lo", type=int, default=10)
+    ap.add_argument("--n-hi", type=int, default=22)
+    ap.add_argument("--batch-seed", type=int, default=4)
+    ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--batch-steps-c128", type=int, default=3)
+    ap.add_argument("--variant", choices=["c64", "c128", "both"], default="both")
+    ap.add_argument("--mem-gb", type=float, default=200.0, help="batched mode: device memory per group")
+    ap.add_argument("--mode", choices=["evolve", "spmv", "chosen", "batched", "precision"], default="evolve",
                     help="evolve: the full measurement; spmv: the SpMV kernel alone; chosen: only the chosen "
                          "form's evolution (for profiling)")
     ap.add_argument("--ref-steps", type=int, default=10, help="time steps the CPU reference arm times at most")
@@ -458,6 +623,12 @@ def main():
         return
     if args.mode == "chosen":
         run_chosen_only(args)
+        return
+    if args.mode == "batched":
+        run_batched(args)
+        return
+    if args.mode == "precision":
+        run_precision(args)
         return
     if world > 1:
         import torch

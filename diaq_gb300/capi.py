@@ -54,10 +54,16 @@ SIGNATURES = {
     "diaq_evolve_launches_per_step": (INT, [P]),
     "diaq_evolve_set_config": (INT, [P, INT, INT]),
     "diaq_evolve_config": (INT, [P, P, P]),
+    "diaq_evolve_set_renormalize": (INT, [P, INT]),
     "diaq_evolve_run_host": (INT, [P, P, P, F64, I64, INT, INT]),
     "diaq_select_sm_min_cost": (INT, [F64, F64, F64, INT, INT, P, P]),
     "diaq_ham_sim_noalloc": (INT, [P, P, P, F64, I64, INT, P, P, P]),
     "diaq_matrix_from_pauli": (INT, [INT, I32, P, P, P, P, INT, P, P]),
+    "diaq_batch_create": (INT, [INT, P, P, P, P, P]),
+    "diaq_batch_destroy": (INT, [P]),
+    "diaq_batch_run": (INT, [P, F64, P, P, I64, P]),
+    "diaq_batch_set_config": (INT, [P, INT, INT]),
+    "diaq_batch_config": (INT, [P, P, P, P]),
     "diaq_mlp_num_params": (INT, []),
     "diaq_mlp_create": (INT, [ctypes.c_uint64, P]),
     "diaq_mlp_destroy": (INT, [P]),
@@ -213,6 +219,9 @@ class Evolve:
         check(lib().diaq_evolve_config(self.h, ctypes.byref(k), ctypes.byref(v)))
         return k.value, v.value
 
+    def set_renormalize(self, on: bool = True):
+        check(lib().diaq_evolve_set_renormalize(self.h, 1 if on else 0))
+
     def launches_per_step(self) -> int:
         return lib().diaq_evolve_launches_per_step(self.h)
 
@@ -259,3 +268,38 @@ class Mlp:
 
     def propose(self, X, s_out, m_out, stream=None):
         check(lib().diaq_mlp_propose(self.h, ptr(X), X.shape[0], ptr(s_out), ptr(m_out), stream))
+
+
+class Batch:
+    """Owning handle of a batched evolution (diaq_batch_t).  Keeps the matrices and the state
+    tensors (lists of torch CUDA float64 tensors, shape (nrhs_i, N_i)) alive."""
+
+    def __init__(self, mats, psi_re, psi_im):
+        self.mats, self.pr, self.pi = list(mats), list(psi_re), list(psi_im)
+        n = len(self.mats)
+        H = (ctypes.c_void_p * n)(*[m.h.value for m in self.mats])
+        k = (ctypes.c_int * n)(*[int(t.shape[0]) for t in self.pr])
+        R = (ctypes.c_void_p * n)(*[t.data_ptr() for t in self.pr])
+        I = (ctypes.c_void_p * n)(*[t.data_ptr() for t in self.pi])
+        out = ctypes.c_void_p()
+        check(lib().diaq_batch_create(n, H, k, R, I, ctypes.byref(out)))
+        self.h = out
+
+    def run(self, dt, s, m, steps, stream=None):
+        n = len(self.mats)
+        sa = (ctypes.c_int * n)(*[int(x) for x in s])
+        ma = (ctypes.c_int * n)(*[int(x) for x in m])
+        check(lib().diaq_batch_run(self.h, dt, sa, ma, steps, stream))
+
+    def set_config(self, states_per_launch: int, rows_per_thread: int = 0):
+        check(lib().diaq_batch_set_config(self.h, states_per_launch, rows_per_thread))
+
+    def config(self):
+        k, v, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().diaq_batch_config(self.h, ctypes.byref(k), ctypes.byref(v), ctypes.byref(p)))
+        return k.value, v.value, p.value
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value and _lib is not None:
+            _lib.diaq_batch_destroy(self.h)
+            self.h = None

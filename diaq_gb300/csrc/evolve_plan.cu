@@ -145,6 +145,52 @@ struct EpiMixed {
     }
 };
 
+// Renormalisation in float64: per state, partial sums of |psi|^2 over row blocks (fixed order),
+// then every block sums its state's partials and scales its rows; in the mixed mode it also
+// refreshes the float32 copy the next step starts from.
+constexpr int kNormBlocks = 256;
+
+__global__ void norm_partial_kernel(const double *__restrict__ pr, const double *__restrict__ pi, int64_t n,
+                                    double *__restrict__ part) {
+    const int q = blockIdx.y;
+    const double *a = pr + (int64_t)q * n, *b = pi + (int64_t)q * n;
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(a[i], a[i], fma(b[i], b[i], s));
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < blockDim.x / 32 ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) part[q * kNormBlocks + blockIdx.x] = v;
+    }
+}
+
+__global__ void renorm_kernel(double *__restrict__ pr, double *__restrict__ pi, float *__restrict__ fr,
+                              float *__restrict__ fi, int64_t n, const double *__restrict__ part) {
+    const int q = blockIdx.y;
+    __shared__ double inv;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int j = 0; j < kNormBlocks; ++j) s += part[q * kNormBlocks + j];
+        inv = s > 0.0 ? 1.0 / sqrt(s) : 1.0;
+    }
+    __syncthreads();
+    const double c = inv;
+    double *a = pr + (int64_t)q * n, *b = pi + (int64_t)q * n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = a[i] * c, y = b[i] * c;
+        a[i] = x;
+        b[i] = y;
+        if (fr) {
+            fr[(int64_t)q * n + i] = (float)x;
+            fi[(int64_t)q * n + i] = (float)y;
+        }
+    }
+}
+
 __global__ void to_f32_kernel(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         b[i] = (float)a[i];
@@ -171,10 +217,13 @@ struct EvolvePlan {
     int launches_per_step = 0;
     SpmvCfg cfg;          // launch shape of the term kernel
     bool tuned = false;   // cfg chosen (by the autotuner or the caller)
+    bool renorm = false;  // rescale every state to norm 1 (float64) after each step
+    double *part = nullptr;  // renormalisation partial sums, nrhs * kNormBlocks
 
     ~EvolvePlan() {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
         if (buf) cudaFree(buf);
+        if (part) cudaFree(part);
         if (Hc) destroy(Hc);
         if (s) cudaStreamDestroy(s);
     }
@@ -209,6 +258,17 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
         return st;
     }
     *out = P;
+    return DIAQ_OK;
+}
+
+static int enqueue_renorm(EvolvePlan &P, double *pr, double *pi, float *fr, float *fi) {
+    if (!P.renorm) return DIAQ_OK;
+    if (!P.part) DQ_CUDA(cudaMalloc(&P.part, sizeof(double) * kNormBlocks * P.nrhs));
+    const dim3 g(kNormBlocks, (unsigned)P.nrhs);
+    norm_partial_kernel<<<g, 256, 0, P.s>>>(pr, pi, P.n, P.part);
+    renorm_kernel<<<g, 256, 0, P.s>>>(pr, pi, fr, fi, P.n, P.part);
+    DQ_CUDA(cudaGetLastError());
+    P.launches_per_step += 2;
     return DIAQ_OK;
 }
 
@@ -256,7 +316,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
             DQ_CUDA(cudaMemcpyAsync(pr, cur_r, sizeof(double) * k * L, cudaMemcpyDeviceToDevice, P.s));
             DQ_CUDA(cudaMemcpyAsync(pi, cur_i, sizeof(double) * k * L, cudaMemcpyDeviceToDevice, P.s));
         }
-        return DIAQ_OK;
+        return enqueue_renorm(P, pr, pi, nullptr, nullptr);
     }
     // MIXED
     float *w = (float *)P.buf;
@@ -290,7 +350,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
         DQ_CUDA(cudaMemcpyAsync(var, in_r, sizeof(float) * k * L, cudaMemcpyDeviceToDevice, P.s));
         DQ_CUDA(cudaMemcpyAsync(vai, in_i, sizeof(float) * k * L, cudaMemcpyDeviceToDevice, P.s));
     }
-    return DIAQ_OK;
+    return enqueue_renorm(P, pr, pi, var, vai);
 }
 
 // ---- autotuner ----------------------------------------------------------------------------------------
@@ -520,6 +580,16 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_
     }
     for (auto &kv : E->graphs) cudaGraphExecDestroy(kv.second);
     E->graphs.clear();
+    return DIAQ_OK;
+}
+
+int diaq_evolve_set_renormalize(diaq_evolve_t E, int on) {
+    if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
+    if (E->renorm != (on != 0)) {
+        E->renorm = on != 0;
+        for (auto &kv : E->graphs) cudaGraphExecDestroy(kv.second);
+        E->graphs.clear();
+    }
     return DIAQ_OK;
 }
 

@@ -50,6 +50,7 @@ typedef enum {
 typedef struct diaq_matrix_s *diaq_matrix_t;
 typedef struct diaq_evolve_s *diaq_evolve_t;
 typedef struct diaq_mlp_s *diaq_mlp_t;
+typedef struct diaq_batch_s *diaq_batch_t;
 
 /* Message of the last failing call on this thread ("" if none). */
 const char *diaq_last_error(void);
@@ -222,6 +223,11 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
 int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread);
 int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread);
 
+/* on != 0: after every step rescale each state to norm 1, the norm computed in float64 (the
+ * exact evolution is unitary; this removes the drift of the truncated series).  Off by default:
+ * the reference's rule does not renormalise. */
+int diaq_evolve_set_renormalize(diaq_evolve_t E, int on);
+
 /* Kernel launches in one recorded time step of the last graph built (0 before any run). */
 int diaq_evolve_launches_per_step(diaq_evolve_t E);
 
@@ -241,6 +247,30 @@ int diaq_select_sm_min_cost(double norm1, double tau, double tol, int max_s, int
  * hamiltonian_simulation_cuda does.  Synchronous. */
 int diaq_ham_sim_host(diaq_matrix_t H, const double *psi0_re, const double *psi0_im, double t,
                       int64_t r, int max_iterations, double *psi_re, double *psi_im);
+
+/* ------------------------------------------------------------------------------------------
+ * Batched evolution: n_inst Hamiltonians of any sizes (all c64 -> float32 terms, or all c128 ->
+ * float64 terms; compensated sums and float64 states either way), instance i with nrhs[i]
+ * states stored at psi_re[i] / psi_im[i] (device, state q at [q*N_i ..]).  One step is one
+ * persistent, work-queued launch per Taylor phase over every instance, recorded as a CUDA graph.
+ * No counterpart in the reference, which evolves one state of one Hamiltonian per call
+ * (src/spHamSim_gpu_all_fused.cu:287-376).  The matrices and state arrays must outlive the batch.
+ * ---------------------------------------------------------------------------------------- */
+int diaq_batch_create(int n_inst, const diaq_matrix_t *H, const int *nrhs, double *const *psi_re,
+                      double *const *psi_im, diaq_batch_t *out);
+int diaq_batch_destroy(diaq_batch_t B);
+
+/* Advance every state by `steps` steps of dt; instance i uses 2^substeps_log2[i] sub-steps of
+ * m[i] terms.  The first run (and any change of dt or schedule) records the step's graph; the
+ * first run also autotunes the launch shape unless one was set.  Asynchronous on stream after
+ * the stream's earlier work has finished. */
+int diaq_batch_run(diaq_batch_t B, double dt, const int *substeps_log2, const int *m, int64_t steps,
+                   void *stream);
+
+/* Force a launch shape (states per launch 1, 2, 4 or 8; rows per thread 1, 2, or 4 for c64), or
+ * 0 states for automatic; and read back the shape and the phases per step. */
+int diaq_batch_set_config(diaq_batch_t B, int states_per_launch, int rows_per_thread);
+int diaq_batch_config(diaq_batch_t B, int *states_per_launch, int *rows_per_thread, int *phases_per_step);
 
 /* ------------------------------------------------------------------------------------------
  * The learned (s, m) proposer: an FP32 MLP 16 -> 64 -> 64 -> 21 + 30 logits (ReLU), trained

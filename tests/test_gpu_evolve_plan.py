@@ -149,3 +149,21 @@ def test_autotuner_caches_its_choice(native, tmp_path, monkeypatch):
     E2 = capi.Evolve(capi.Matrix.create(A.rows, A.cols, A.off, A.re, A.im), 4, capi.EVOLVE_MIXED)
     E2.run(pr, pi, A.rows, 0.05, 1, 0, 12)
     assert E2.config() == (k, v)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_renormalize(native, mode):
+    """With renormalisation every state leaves each step with norm 1 (float64), and the states
+    stay within the form's tolerance of the oracle."""
+    import torch
+
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 10, 2, mode)
+    E.set_renormalize(True)
+    E.run(pr, pi, A.rows, 0.1, 6, 0, 8)    # few terms: the series alone would lose norm
+    got = _result(pr, pi)
+    norms = np.linalg.norm(got, axis=1)
+    assert np.abs(norms - 1).max() < 1e-12
+    want = orc.ham_sim(A, P[1], 0.6, 6, 8)
+    want = want / np.linalg.norm(want)
+    assert np.linalg.norm(got[1] - want) < (1e-12 if mode == 0 else 1e-6)
