@@ -296,6 +296,9 @@ def run_chosen_only(args):
     capi.check(L.diaq_norm1_est(H.h, ctypes.byref(norm1), None))
     s_c, m_c, _ = chosen_schedule(capi, H, norm1.value)
     E = capi.Evolve(H, args.states, capi.EVOLVE_MIXED)
+    if args.shape:
+        k, v, p = (int(x) for x in args.shape.split(","))
+        E.set_config(k, v, bool(p))
     P0 = ham.random_state(N, 0, k=args.states) if args.states > 1 else ham.random_state(N, 0)[None, :]
     pr = torch.from_numpy(np.ascontiguousarray(P0.real)).cuda()
     pi = torch.from_numpy(np.ascontiguousarray(P0.imag)).cuda()
@@ -303,6 +306,7 @@ def run_chosen_only(args):
     E.run(pr, pi, N, DT, args.warmup, s_c, m_c, sp)
     ms = _timed(torch.cuda.current_stream(), lambda: E.run(pr, pi, N, DT, args.steps, s_c, m_c, sp))
     print(json.dumps({"mode": "chosen", "n_qubits": args.n, "states": args.states, "s": s_c, "m": m_c,
+                      "shape": list(E.config()) + [E.pipelined()],
                       "ms_per_step": ms / args.steps, "us_per_launch": 1e3 * ms / args.steps / E.launches_per_step()}),
           flush=True)
 
@@ -382,6 +386,8 @@ def run_batched(args):
             small = [j for j, idx in enumerate(grp) if specs[idx][1] <= 12][:3]
             start = {j: (prs[j][0].cpu().numpy() + 1j * pis[j][0].cpu().numpy()) for j in small}
             B = capi.Batch(mats, prs, pis)
+            if variant == "c128":
+                B.set_config(4, 2)   # FP64-bound either way; autotuning would cost minutes of steps
             stream = torch.cuda.current_stream()
             B.run(dt, sched_s, sched_m, args.warmup, stream.cuda_stream)
             torch.cuda.synchronize()
@@ -597,6 +603,7 @@ def main():
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--spmv-reps", type=int, default=1000)
     ap.add_argument("--states", type=int, default=8, help="states evolved together by the chosen form")
+    ap.add_argument("--shape", default="", help="chosen mode: force the launch shape 'states,rows,pipelined'")
     ap.add_argument("--instances", type=int, default=512, help="batched mode: Hamiltonians")
     ap.add_argument("--n-lo", type=int, default=10)
     ap.add_argument("--n-hi", type=int, default=22)

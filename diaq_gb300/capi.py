@@ -52,8 +52,8 @@ SIGNATURES = {
     "diaq_evolve_destroy": (INT, [P]),
     "diaq_evolve_run": (INT, [P, P, P, I64, F64, I64, INT, INT, P]),
     "diaq_evolve_launches_per_step": (INT, [P]),
-    "diaq_evolve_set_config": (INT, [P, INT, INT]),
-    "diaq_evolve_config": (INT, [P, P, P]),
+    "diaq_evolve_set_config": (INT, [P, INT, INT, INT]),
+    "diaq_evolve_config": (INT, [P, P, P, P]),
     "diaq_evolve_set_renormalize": (INT, [P, INT]),
     "diaq_evolve_run_host": (INT, [P, P, P, F64, I64, INT, INT]),
     "diaq_select_sm_min_cost": (INT, [F64, F64, F64, INT, INT, P, P]),
@@ -210,14 +210,20 @@ class Evolve:
         """In place on host float64 arrays of nrhs*N values."""
         check(lib().diaq_evolve_run_host(self.h, psi_re.ctypes.data, psi_im.ctypes.data, dt, steps, substeps_log2, m))
 
-    def set_config(self, states_per_launch: int, rows_per_thread: int = 0):
+    def set_config(self, states_per_launch: int, rows_per_thread: int = 0, pipelined: bool = False):
         """Force a launch shape (0 states: automatic, autotuned on the next run)."""
-        check(lib().diaq_evolve_set_config(self.h, states_per_launch, rows_per_thread))
+        check(lib().diaq_evolve_set_config(self.h, states_per_launch, rows_per_thread, 1 if pipelined else 0))
 
     def config(self):
-        k, v = ctypes.c_int(), ctypes.c_int()
-        check(lib().diaq_evolve_config(self.h, ctypes.byref(k), ctypes.byref(v)))
+        """(states per launch, rows per thread) of the current shape."""
+        k, v, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().diaq_evolve_config(self.h, ctypes.byref(k), ctypes.byref(v), ctypes.byref(p)))
         return k.value, v.value
+
+    def pipelined(self) -> bool:
+        k, v, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().diaq_evolve_config(self.h, ctypes.byref(k), ctypes.byref(v), ctypes.byref(p)))
+        return bool(p.value)
 
     def set_renormalize(self, on: bool = True):
         check(lib().diaq_evolve_set_renormalize(self.h, 1 if on else 0))

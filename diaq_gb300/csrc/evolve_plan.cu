@@ -27,7 +27,7 @@
 #include <string>
 #include <tuple>
 
-#include "spmv_kernel.cuh"
+#include "spmv_pipe.cuh"
 
 namespace diaq_gb300 {
 
@@ -340,7 +340,10 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
             e.scale = (float)(tau / (double)t);
             e.first = (t == 1);
             e.last = (t == m);
-            DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiMixed, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg)));
+            if (P.cfg.pipe)
+                DQ_TRY(launch_dia_spmv_pipe<EpiMixed>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg.kmax));
+            else
+                DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiMixed, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg)));
             ++P.launches_per_step;
             std::swap(in_r, out_r);
             std::swap(in_i, out_i);
@@ -365,9 +368,9 @@ static std::string cache_path() {
     return std::string(home ? home : "/tmp") + "/.cache/diaq_gb300/autotune.json";
 }
 
-// The cache is a flat JSON object {"key": [kmax, vr], ...}.
-static std::map<std::string, std::pair<int, int>> read_cache() {
-    std::map<std::string, std::pair<int, int>> out;
+// The cache is a flat JSON object {"key": [states_per_launch, rows_per_thread, pipelined], ...}.
+static std::map<std::string, SpmvCfg> read_cache() {
+    std::map<std::string, SpmvCfg> out;
     std::ifstream f(cache_path());
     if (!f) return out;
     std::stringstream ss;
@@ -378,17 +381,17 @@ static std::map<std::string, std::pair<int, int>> read_cache() {
         const size_t j = t.find('"', i + 1);
         if (j == std::string::npos) break;
         const std::string key = t.substr(i + 1, j - i - 1);
-        int a = 0, b = 0;
+        int a = 0, b = 0, c = 0;
         const size_t br = t.find('[', j);
-        if (br == std::string::npos || std::sscanf(t.c_str() + br, "[%d ,%d]", &a, &b) != 2) break;
-        out[key] = {a, b};
+        if (br == std::string::npos || std::sscanf(t.c_str() + br, "[%d ,%d ,%d]", &a, &b, &c) < 2) break;
+        out[key] = SpmvCfg{a, b, c};
         i = t.find(']', br);
         if (i == std::string::npos) break;
     }
     return out;
 }
 
-static void write_cache(const std::map<std::string, std::pair<int, int>> &c) {
+static void write_cache(const std::map<std::string, SpmvCfg> &c) {
     const std::string path = cache_path();
     const size_t slash = path.rfind('/');
     if (slash != std::string::npos) {
@@ -401,7 +404,9 @@ static void write_cache(const std::map<std::string, std::pair<int, int>> &c) {
     if (!f) return;
     f << "{\n";
     size_t n = 0;
-    for (const auto &kv : c) f << "  \"" << kv.first << "\": [" << kv.second.first << ", " << kv.second.second << "]" << (++n < c.size() ? ",\n" : "\n");
+    for (const auto &kv : c)
+        f << "  \"" << kv.first << "\": [" << kv.second.kmax << ", " << kv.second.vr << ", " << kv.second.pipe << "]"
+          << (++n < c.size() ? ",\n" : "\n");
     f << "}\n";
     f.close();
     std::rename((path + ".tmp").c_str(), path.c_str());
@@ -424,9 +429,10 @@ static std::string tune_key(const EvolvePlan &P, int sl, int m) {
 static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double *pi, int64_t ld, cudaStream_t user) {
     std::vector<SpmvCfg> cand;
     if (P.mode == DIAQ_EVOLVE_MIXED)
-        cand = {{8, 1}, {8, 2}, {8, 4}, {4, 2}, {4, 4}, {2, 4}, {1, 4}};
+        cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
+                {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1}};
     else
-        cand = {{8, 1}, {8, 2}, {4, 2}, {2, 2}, {1, 2}};
+        cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
     int kcap = 1;
     while (kcap < P.nrhs && kcap < 8) kcap *= 2;
@@ -438,7 +444,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     auto cache = read_cache();
     auto hit = cache.find(key);
     if (hit != cache.end()) {
-        P.cfg = SpmvCfg{hit->second.first, hit->second.second};
+        P.cfg = hit->second;
         P.tuned = true;
         return DIAQ_OK;
     }
@@ -494,7 +500,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     if (st != DIAQ_OK) return st;
     P.cfg = best_cfg;
     P.tuned = true;
-    cache[key] = {best_cfg.kmax, best_cfg.vr};
+    cache[key] = best_cfg;
     write_cache(cache);
     return DIAQ_OK;
 }
@@ -565,7 +571,7 @@ int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld,
 
 int diaq_evolve_launches_per_step(diaq_evolve_t E) { return E ? E->launches_per_step : 0; }
 
-int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread) {
+int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread, int pipelined) {
     if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
     if (states_per_launch == 0) {  // back to automatic choice
         E->tuned = false;
@@ -575,7 +581,9 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_launch < 1 || states_per_launch > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_launch in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
-        E->cfg = SpmvCfg{states_per_launch, rows_per_thread};
+        if (pipelined && !(f32 && rows_per_thread == 4))
+            return set_error(DIAQ_ERR_INVALID, "evolve: the pipelined kernel is the mixed mode's, with 4 rows per thread");
+        E->cfg = SpmvCfg{states_per_launch, rows_per_thread, pipelined ? 1 : 0};
         E->tuned = true;
     }
     for (auto &kv : E->graphs) cudaGraphExecDestroy(kv.second);
@@ -593,10 +601,11 @@ int diaq_evolve_set_renormalize(diaq_evolve_t E, int on) {
     return DIAQ_OK;
 }
 
-int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread) {
+int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread, int *pipelined) {
     if (!E || !states_per_launch || !rows_per_thread) return set_error(DIAQ_ERR_INVALID, "NULL argument");
     *states_per_launch = E->cfg.kmax;
     *rows_per_thread = E->cfg.vr > 0 ? E->cfg.vr : (E->mode == DIAQ_EVOLVE_MIXED ? 4 : 2);
+    if (pipelined) *pipelined = E->cfg.pipe;
     return DIAQ_OK;
 }
 

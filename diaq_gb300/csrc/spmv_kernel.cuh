@@ -237,6 +237,7 @@ inline unsigned spmv_blocks(int64_t rows, int V) {
 struct SpmvCfg {
     int kmax = 8;
     int vr = 0;
+    int pipe = 0;  // 1: the cp.async-pipelined float kernel (4 rows per thread)
 };
 
 template <typename T, int K, class Epi, int VR, int... More>

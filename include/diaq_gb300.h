@@ -216,12 +216,14 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
                          int substeps_log2, int m);
 
 /* Launch shape of the plan's term kernel: states per launch (1..8; the matrix is read once per
- * launch) and rows per thread (1, 2, or 4 for the mixed mode).  0 states = choose automatically:
- * on the first run the autotuner times the candidate shapes on two steps of scratch copies of
- * the states and keeps the fastest, caching the choice in a JSON file (DIAQ_AUTOTUNE_CACHE, else
- * $HOME/.cache/diaq_gb300/autotune.json).  Setting a shape drops the recorded graphs. */
-int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread);
-int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread);
+ * launch), rows per thread (1, 2, or 4 for the mixed mode) and, for the mixed mode with 4 rows,
+ * pipelined != 0 to stream the next diagonals through shared memory with asynchronous copies.
+ * 0 states = choose automatically: on the first run the autotuner times the candidate shapes on
+ * two steps of scratch copies of the states and keeps the fastest, caching the choice in a JSON
+ * file (DIAQ_AUTOTUNE_CACHE, else $HOME/.cache/diaq_gb300/autotune.json).  Setting a shape drops
+ * the recorded graphs.  pipelined may be NULL in diaq_evolve_config. */
+int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread, int pipelined);
+int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread, int *pipelined);
 
 /* on != 0: after every step rescale each state to norm 1, the norm computed in float64 (the
  * exact evolution is unitary; this removes the drift of the truncated series).  Off by default:

@@ -103,14 +103,15 @@ def test_plan_rejects_bad_input(native):
         capi.Evolve(S, 1)
 
 
-@pytest.mark.parametrize("cfg", [(8, 1), (8, 2), (8, 4), (4, 2), (4, 4), (2, 4), (1, 4), (1, 1)])
+@pytest.mark.parametrize("cfg", [(8, 1, 0), (8, 2, 0), (8, 4, 0), (4, 2, 0), (4, 4, 0), (2, 4, 0), (1, 4, 0),
+                                 (1, 1, 0), (8, 4, 1), (4, 4, 1), (2, 4, 1), (1, 4, 1)])
 def test_mixed_every_launch_shape(native, cfg):
-    """Each (states per launch, rows per thread) shape the autotuner may pick gives the same
-    answer (odd sizes: 3 states, 2^11 + rows from a rectangular-free square chain)."""
+    """Each (states per launch, rows per thread, pipelined) shape the autotuner may pick gives
+    the same answer (3 states: the last launch of a chunked shape runs with masked slots)."""
     capi, _ = native
     A, E, P, pr, pi = _setup(capi, 11, 3, capi.EVOLVE_MIXED)
     E.set_config(*cfg)
-    assert E.config() == cfg
+    assert E.config() == cfg[:2] and E.pipelined() == bool(cfg[2])
     E.run(pr, pi, A.rows, 0.05, 5, 0, 13)
     got = _result(pr, pi)
     for q in range(3):
@@ -140,7 +141,7 @@ def test_autotuner_caches_its_choice(native, tmp_path, monkeypatch):
     import json
 
     saved = json.load(open(cache))
-    assert any(val == [k, v] for val in saved.values())
+    assert any(val[:2] == [k, v] for val in saved.values())
     # the tuning ran on scratch copies: the states advanced exactly 2 steps
     got = _result(pr, pi)
     want = orc.ham_sim(A, P[2], 0.1, 2, 12)
@@ -167,3 +168,16 @@ def test_renormalize(native, mode):
     want = orc.ham_sim(A, P[1], 0.6, 6, 8)
     want = want / np.linalg.norm(want)
     assert np.linalg.norm(got[1] - want) < (1e-12 if mode == 0 else 1e-6)
+
+
+def test_pipelined_large_unaligned_offsets(native):
+    """The pipelined kernel on the 16-qubit XXZ chain: offsets +-1, +-2 and +-(2^15 - 1) take the
+    element-wise copies, the rest the 16-byte ones; 5 states = one full and one masked chunk."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 16, 5, capi.EVOLVE_MIXED)
+    E.set_config(4, 4, True)
+    E.run(pr, pi, A.rows, 0.05, 2, 0, 10)
+    got = _result(pr, pi)
+    for q in (0, 4):
+        want = orc.ham_sim(A, P[q], 0.1, 2, 10)
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
