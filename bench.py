@@ -241,26 +241,34 @@ def run_spmv_only(args):
     N, off, re, im = workload(args.n)
     H = capi.Matrix.create(N, N, off, re, im)
     Hc = H.convert(capi.C64)
+    Hf = H.convert(capi.C128F2)
     psi = ham.random_state(N, 0)
     sp = torch.cuda.current_stream().cuda_stream
     out = {}
-    for name, M, dt, fn in (("c128", H, torch.float64, L.diaq_spmv_z), ("c64", Hc, torch.float32, L.diaq_spmv_c)):
+    for name, M, dt, fn in (("c128", H, torch.float64, L.diaq_spmv_z), ("c64", Hc, torch.float32, L.diaq_spmv_c),
+                            ("c128f2", Hf, torch.float64, L.diaq_spmv_z)):
         xr = torch.from_numpy(psi.real.copy()).to("cuda", dt)
         xi = torch.from_numpy(psi.imag.copy()).to("cuda", dt)
         yr, yi = torch.empty_like(xr), torch.empty_like(xi)
         for _ in range(args.warmup):
             capi.check(fn(M.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
 
-        def loop():
-            for i in range(args.spmv_reps):
-                a, b, c, d = (xr, xi, yr, yi) if i % 2 == 0 else (yr, yi, xr, xi)
-                capi.check(fn(M.h, a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), sp))
+        def loop():   # y = A x from the same x each time (float pairs overflow above ~1e38)
+            for _ in range(args.spmv_reps):
+                capi.check(fn(M.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
 
         torch.cuda.synchronize()
         us = 1e3 * _timed(torch.cuda.current_stream(), loop) / args.spmv_reps
-        w = 16 if name == "c128" else 8
+        w = 8 if name == "c64" else 16
         by = w * int(re.size) + 2 * w * N
         out[name] = {"us": us, "gbs": by / us / 1e3, "bytes": by}
+        if name == "c128f2":   # error of the float-pair product against the float64 one
+            y64r, y64i = torch.empty_like(xr), torch.empty_like(xi)
+            capi.check(L.diaq_spmv_z(H.h, xr.data_ptr(), xi.data_ptr(), y64r.data_ptr(), y64i.data_ptr(), sp))
+            capi.check(fn(M.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
+            torch.cuda.synchronize()
+            d = torch.maximum((yr - y64r).abs().max(), (yi - y64i).abs().max())
+            out[name]["maxrel_vs_c128"] = float(d / torch.maximum(y64r.abs().max(), y64i.abs().max()))
     print(json.dumps({"mode": "spmv", "n_qubits": args.n, **out}), flush=True)
 
 
@@ -298,7 +306,7 @@ def run_chosen_only(args):
     E = capi.Evolve(H, args.states, capi.EVOLVE_MIXED)
     if args.shape:
         k, v, p = (int(x) for x in args.shape.split(","))
-        E.set_config(k, v, bool(p))
+        E.set_config(k, v, p)
     P0 = ham.random_state(N, 0, k=args.states) if args.states > 1 else ham.random_state(N, 0)[None, :]
     pr = torch.from_numpy(np.ascontiguousarray(P0.real)).cuda()
     pi = torch.from_numpy(np.ascontiguousarray(P0.imag)).cuda()
@@ -551,6 +559,26 @@ def run_ours(args, rank, world):
 
     spmv_us = 1e3 * _timed(stream, spmv_loop) / args.spmv_reps
 
+    # ---- the same SpMV on a c128f2 copy (float-pair values, FP32 pipes) ----
+    Hf = H.convert(capi.C128F2)
+
+    xr.copy_(ppr)
+    xi.copy_(ppi)
+
+    def spmv_f2_loop():   # y = A x from the same x each time: float pairs hold magnitudes up to ~1e38 only
+        for _ in range(args.spmv_reps):
+            capi.check(L.diaq_spmv_z(Hf.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
+
+    spmv_f2_loop()
+    spmv_f2_us = 1e3 * _timed(stream, spmv_f2_loop) / args.spmv_reps
+    y64r, y64i = torch.empty_like(xr), torch.empty_like(xi)
+    capi.check(L.diaq_spmv_z(H.h, xr.data_ptr(), xi.data_ptr(), y64r.data_ptr(), y64i.data_ptr(), sp))
+    capi.check(L.diaq_spmv_z(Hf.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
+    torch.cuda.synchronize()
+    f2_err = float(torch.maximum((yr - y64r).abs().max(), (yi - y64i).abs().max())
+                   / torch.maximum(y64r.abs().max(), y64i.abs().max()))
+    del Hf, y64r, y64i
+
     peak, peak_kind = peaks()
     # algorithmic bytes of one chosen time step: per launch the c64 matrix once, per state
     # v in (8N) + v out (8N) + sum pair read/write (16N each; the first term only writes, the
@@ -568,7 +596,8 @@ def run_ours(args, rank, world):
         "config": {"workload": f"xxz{args.n}_periodic_evolve", "form": "chosen", "n_qubits": args.n, "rows": N,
                    "ndiag": len(off), "stored_values": total, "dt": DT, "states_per_gpu": S,
                    "substeps": 1 << s_c, "taylor_terms": m_c, "selection": selection,
-                   "launch_shape": {"states_per_launch": chosen.config()[0], "rows_per_thread": chosen.config()[1]},
+                   "launch_shape": {"states_per_launch": chosen.config()[0], "rows_per_thread": chosen.config()[1],
+                                    "kernel_variant": chosen.pipelined()},
                    "tol_per_step": TOL_STEP, "norm1": norm1.value,
                    "l2": "inputs larger than L2 (c64 matrix 327 MB, states 128 MB > 129 MB)",
                    "parallelism": f"replicas{world}"},
@@ -582,6 +611,10 @@ def run_ours(args, rank, world):
         "spmv_c128": {"us": spmv_us, "gbs": (16 * total + 32 * N) / spmv_us / 1e3,
                       "frac": (16 * total + 32 * N) / spmv_us / 1e3 / peak,
                       "dfma_per_launch": 4 * total, "reps": args.spmv_reps},
+        "spmv_c128f2": {"us": spmv_f2_us, "gbs": (16 * total + 32 * N) / spmv_f2_us / 1e3,
+                        "frac": (16 * total + 32 * N) / spmv_f2_us / 1e3 / peak,
+                        "maxrel_vs_c128": f2_err, "reps": args.spmv_reps,
+                        "note": "same matrix as float pairs (DIAQ_C128F2), float64 vectors; includes the split of x"},
         "e2e": {"value": world * S * K / e2e_s, "unit": "states·steps/s", "h2d_bytes_per_step": 16 * N * S / K,
                 "d2h_bytes_per_step": 16 * N * S / K,
                 "note": "diaq_evolve_run_host: S states up, K steps, S states down, in the timed region"},

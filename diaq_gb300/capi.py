@@ -15,7 +15,7 @@ import numpy as np
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libdiaq_gb300.so")
 
-C128, C64 = 0, 1
+C128, C64, C128F2 = 0, 1, 2
 EVOLVE_C128, EVOLVE_MIXED = 0, 1
 _lib = None
 
@@ -37,6 +37,7 @@ SIGNATURES = {
     "diaq_spmm": (INT, [P, INT, P, P, I64, P, P, I64, P]),
     "diaq_spmv_host": (INT, [P, P, P, P, P]),
     "diaq_spmv_ntimes_host": (INT, [P, P, P, INT, P, P]),
+    "diaq_spmm_dia_device": (INT, [P, P, INT, I64, I64, P, I64, P, INT, P]),
     "diaq_spgemm_symbolic": (INT, [P, P, P, P, P]),
     "diaq_spgemm_numeric": (INT, [P, P, P, P]),
     "diaq_spgemm": (INT, [P, P, INT, P, P]),
@@ -210,9 +211,11 @@ class Evolve:
         """In place on host float64 arrays of nrhs*N values."""
         check(lib().diaq_evolve_run_host(self.h, psi_re.ctypes.data, psi_im.ctypes.data, dt, steps, substeps_log2, m))
 
-    def set_config(self, states_per_launch: int, rows_per_thread: int = 0, pipelined: bool = False):
-        """Force a launch shape (0 states: automatic, autotuned on the next run)."""
-        check(lib().diaq_evolve_set_config(self.h, states_per_launch, rows_per_thread, 1 if pipelined else 0))
+    def set_config(self, states_per_launch: int, rows_per_thread: int = 0, pipelined: int = 0):
+        """Force a launch shape (0 states: automatic, autotuned on the next run).  pipelined: 0
+        registers only, 1 cp.async pipeline, 2 / 3 / 4 shuffled state windows with an L2 prefetch of
+        the matrix 4 / 8 / 0 diagonals ahead."""
+        check(lib().diaq_evolve_set_config(self.h, states_per_launch, rows_per_thread, int(pipelined)))
 
     def config(self):
         """(states per launch, rows per thread) of the current shape."""
@@ -220,10 +223,11 @@ class Evolve:
         check(lib().diaq_evolve_config(self.h, ctypes.byref(k), ctypes.byref(v), ctypes.byref(p)))
         return k.value, v.value
 
-    def pipelined(self) -> bool:
+    def pipelined(self) -> int:
+        """The kernel variant of the current shape (0 registers, 1 cp.async, 2-4 shuffled windows)."""
         k, v, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(lib().diaq_evolve_config(self.h, ctypes.byref(k), ctypes.byref(v), ctypes.byref(p)))
-        return bool(p.value)
+        return p.value
 
     def set_renormalize(self, on: bool = True):
         check(lib().diaq_evolve_set_renormalize(self.h, 1 if on else 0))

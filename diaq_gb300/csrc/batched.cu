@@ -481,6 +481,7 @@ int diaq_batch_create(int n_inst, const diaq_matrix_t *H, const int *nrhs, doubl
         if (!H[i] || !psi_re[i] || !psi_im[i]) return set_error(DIAQ_ERR_INVALID, "batch: NULL matrix or state pointer");
         if (H[i]->rows != H[i]->cols) return set_error(DIAQ_ERR_INVALID, "batch: every H must be square");
         if (H[i]->prec != prec) return set_error(DIAQ_ERR_INVALID, "batch: all matrices must have the same precision");
+        if (prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "batch: c128 or c64 matrices only");
         if (nrhs[i] < 1) return set_error(DIAQ_ERR_INVALID, "batch: every instance needs at least one state");
         work_elems += (size_t)nrhs[i] * (size_t)H[i]->rows;
     }

@@ -38,7 +38,7 @@ static_assert(sizeof(DiagMeta) == 48, "DiagMeta layout");
 struct Matrix {
     int64_t rows = 0, cols = 0;
     int32_t nd = 0;
-    int prec = DIAQ_C128;                  // DIAQ_C128 (double) or DIAQ_C64 (float)
+    int prec = DIAQ_C128;                  // DIAQ_C128 (double), DIAQ_C64 (float), DIAQ_C128F2 (float pairs)
     std::vector<int32_t> off;              // host copies, slot order
     std::vector<DiagMeta> meta;
     int64_t capacity = 0;                  // values allocated per array
@@ -47,7 +47,8 @@ struct Matrix {
     DiagMeta *d_meta = nullptr;            // device copy of meta
     int device = 0;
 
-    size_t elem() const { return prec == DIAQ_C128 ? sizeof(double) : sizeof(float); }
+    // bytes per stored value and array (C128F2: a hi and a lo float, in two planes)
+    size_t elem() const { return prec == DIAQ_C64 ? sizeof(float) : sizeof(double); }
 };
 
 // ---- error state -------------------------------------------------------------------------
@@ -91,6 +92,12 @@ int taylor_term_launch(const Matrix &A, const void *tin_r, const void *tin_i, vo
                        const void *init_i, double scale, int nrhs, int64_t ld, cudaStream_t s);
 
 int num_sms();
+
+// DIAQ_C128F2 (spmv_f2.cu)
+int f2_scatter(Matrix &M, const double *re, const double *im, cudaStream_t s);
+int f2_gather(const Matrix &M, double *re, double *im, cudaStream_t s);
+int f2_convert(const Matrix &src, Matrix &dst, cudaStream_t s);
+int f2_spmv(const Matrix &A, const double *xr, const double *xi, double *yr, double *yi, cudaStream_t s);
 
 // Copy of A in precision prec / A without its exact-zero diagonals (new matrices).
 int copy_as(const Matrix &A, int prec, cudaStream_t s, Matrix **out);

@@ -39,7 +39,7 @@ struct EpiPlain {
     double *outr, *outi;          // sum out
     int64_t ld;
     double scale;
-    EpiPlain shifted(int q0) const {
+    __host__ __device__ EpiPlain shifted(int q0) const {
         EpiPlain e = *this;
         const int64_t o = q0 * ld;
         if (e.tr) {
@@ -90,7 +90,7 @@ struct EpiMixed {
     int64_t ld;
     float scale;
     int first, last;
-    EpiMixed shifted(int q0) const {
+    __host__ __device__ EpiMixed shifted(int q0) const {
         EpiMixed e = *this;
         const int64_t o = q0 * ld;
         e.vr += o;
@@ -114,6 +114,8 @@ struct EpiMixed {
                 const int64_t i = q * ld + r;
                 const float tr = si[q][v] * scale, ti = -sr[q][v] * scale;
                 float h_r, h_i, l_r, l_i;
+                // plain loads and stores: part of the sums stays in L2 until the next launch reads
+                // it (streaming them with evict-first hints measured 20 % slower)
                 if (first) {
                     h_r = tr;
                     h_i = ti;
@@ -340,11 +342,16 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
             e.scale = (float)(tau / (double)t);
             e.first = (t == 1);
             e.last = (t == m);
-            if (P.cfg.pipe)
-                DQ_TRY(launch_dia_spmv_pipe<EpiMixed>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg.kmax));
-            else
+            if (P.cfg.pipe >= 2) {
+                DQ_TRY(launch_dia_spmv_pf<EpiMixed>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg.kmax, P.cfg.pipe,
+                                                    &P.launches_per_step));
+            } else if (P.cfg.pipe) {
+                DQ_TRY(launch_dia_spmv_pipe<EpiMixed>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg.kmax,
+                                                      &P.launches_per_step));
+            } else {
                 DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiMixed, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg)));
-            ++P.launches_per_step;
+                ++P.launches_per_step;  // one launch over all states
+            }
             std::swap(in_r, out_r);
             std::swap(in_i, out_i);
         }
@@ -430,7 +437,9 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     std::vector<SpmvCfg> cand;
     if (P.mode == DIAQ_EVOLVE_MIXED)
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
-                {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1}};
+                {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
+                {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}};
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -581,9 +590,12 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_launch < 1 || states_per_launch > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_launch in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
+        if (pipelined < 0 || pipelined > 4)
+            return set_error(DIAQ_ERR_INVALID,
+                             "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), 4 (shuffled windows)");
         if (pipelined && !(f32 && rows_per_thread == 4))
-            return set_error(DIAQ_ERR_INVALID, "evolve: the pipelined kernel is the mixed mode's, with 4 rows per thread");
-        E->cfg = SpmvCfg{states_per_launch, rows_per_thread, pipelined ? 1 : 0};
+            return set_error(DIAQ_ERR_INVALID, "evolve: the pipelined kernels are the mixed mode's, with 4 rows per thread");
+        E->cfg = SpmvCfg{states_per_launch, rows_per_thread, pipelined};
         E->tuned = true;
     }
     for (auto &kv : E->graphs) cudaGraphExecDestroy(kv.second);

@@ -83,6 +83,7 @@ __global__ void sum_partials_kernel(const double *__restrict__ part, int n, doub
 }
 
 int norm1_est(const Matrix &A, double *out, cudaStream_t s) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "norm1_est: convert a c128f2 matrix to c128 first");
     *out = 0.0;
     if (A.nd == 0 || A.cols == 0) return DIAQ_OK;
     unsigned long long *d = nullptr;
@@ -106,6 +107,7 @@ int norm1_est(const Matrix &A, double *out, cudaStream_t s) {
 }
 
 int frobenius(const Matrix &A, double *out, cudaStream_t s) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "frobenius: convert a c128f2 matrix to c128 first");
     *out = 0.0;
     if (A.capacity == 0) return DIAQ_OK;
     const int nblk = (int)std::min<int64_t>((A.capacity + 255) / 256, 2 * num_sms());
@@ -324,6 +326,7 @@ int single_diag_exp(const Matrix &A, int negative, double t, cudaStream_t s, Mat
 
 // ---- pow ------------------------------------------------------------------------------------------
 int pow_matrix(const Matrix &A, int n, bool prune, cudaStream_t s, Matrix **out) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "pow: convert a c128f2 matrix to c128 first");
     if (n < 0) return set_error(DIAQ_ERR_INVALID, "pow: negative exponent not supported");
     if (A.rows != A.cols) return set_error(DIAQ_ERR_INVALID, "pow: matrix must be square");
     if (n == 0) return identity(A.rows, A.prec, s, out);
@@ -419,6 +422,7 @@ static int taylor(const Matrix &X, int max_it, double tol, bool prune, cudaStrea
 
 int expm_negative(const Matrix &A, double t, int max_it, double cutoff, double tol, bool prune, cudaStream_t s,
                   Matrix **out, int *s_out, int *terms_out) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "expm_negative: convert a c128f2 matrix to c128 first");
     if (A.rows != A.cols) return set_error(DIAQ_ERR_INVALID, "expm_negative: matrix must be square");
     if (s_out) *s_out = 0;
     if (terms_out) *terms_out = 0;
@@ -447,6 +451,7 @@ int expm_negative(const Matrix &A, double t, int max_it, double cutoff, double t
 }
 
 int expm(const Matrix &A, int max_it, double cutoff, double tol, bool prune, cudaStream_t s, Matrix **out) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "expm: convert a c128f2 matrix to c128 first");
     if (A.rows != A.cols) return set_error(DIAQ_ERR_INVALID, "expm: matrix must be square");
     if (A.nd == 1) return single_diag_exp(A, 0, 0.0, s, out);
     double nrm = 0.0;

@@ -89,7 +89,8 @@ int plan_layout(Matrix &M, int64_t rows, int64_t cols, int32_t nd, const int32_t
         cursor = s + len;
         pstart += len;
     }
-    M.capacity = cursor + kAlign;
+    // a multiple of kAlign, so that a second plane (C128F2) starts aligned as well
+    M.capacity = (cursor + 2 * kAlign - 1) / kAlign * kAlign;
     M.total = pstart;
     return DIAQ_OK;
 }
@@ -121,8 +122,8 @@ void release(Matrix &M) {
 
 int make_zero(int64_t rows, int64_t cols, int32_t nd, const int32_t *off, int prec,
               cudaStream_t s, Matrix **out) {
-    if (prec != DIAQ_C128 && prec != DIAQ_C64)
-        return set_error(DIAQ_ERR_INVALID, "precision must be DIAQ_C128 or DIAQ_C64");
+    if (prec != DIAQ_C128 && prec != DIAQ_C64 && prec != DIAQ_C128F2)
+        return set_error(DIAQ_ERR_INVALID, "precision must be DIAQ_C128, DIAQ_C64 or DIAQ_C128F2");
     Matrix *M = new diaq_matrix_s();
     M->prec = prec;
     int st = plan_layout(*M, rows, cols, nd, off);
@@ -217,6 +218,7 @@ static dim3 diag_grid(const Matrix &M) {
 
 int scatter_packed(Matrix &M, const double *re, const double *im, cudaStream_t s) {
     if (M.nd == 0 || M.total == 0) return DIAQ_OK;
+    if (M.prec == DIAQ_C128F2) return f2_scatter(M, re, im, s);
     const dim3 g = diag_grid(M);
     if (M.prec == DIAQ_C128)
         scatter_kernel<double, double><<<g, 256, 0, s>>>(M.d_meta, M.nd, re, im, (double *)M.re, (double *)M.im);
@@ -228,6 +230,7 @@ int scatter_packed(Matrix &M, const double *re, const double *im, cudaStream_t s
 
 int gather_packed(const Matrix &M, double *re, double *im, cudaStream_t s) {
     if (M.nd == 0 || M.total == 0) return DIAQ_OK;
+    if (M.prec == DIAQ_C128F2) return f2_gather(M, re, im, s);
     const dim3 g = diag_grid(M);
     if (M.prec == DIAQ_C128)
         gather_kernel<double><<<g, 256, 0, s>>>(M.d_meta, M.nd, (const double *)M.re, (const double *)M.im, re, im);
@@ -261,7 +264,16 @@ static int remap(const Matrix &src, Matrix &dst, const int32_t *d_map, cudaStrea
 int copy_as(const Matrix &A, int prec, cudaStream_t s, Matrix **out) {
     Matrix *C = nullptr;
     DQ_TRY(make_zero(A.rows, A.cols, A.nd, A.off.data(), prec, s, &C));
-    int st = remap(A, *C, nullptr, s);
+    int st = DIAQ_OK;
+    if (A.prec == DIAQ_C128F2 && prec == DIAQ_C128F2) {
+        cudaError_t e = cudaMemcpyAsync(C->re, A.re, A.capacity * A.elem(), cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(C->im, A.im, A.capacity * A.elem(), cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) st = cuda_status(e, "copy", __FILE__, __LINE__);
+    } else if (A.prec == DIAQ_C128F2 || prec == DIAQ_C128F2) {
+        st = f2_convert(A, *C, s);
+    } else {
+        st = remap(A, *C, nullptr, s);
+    }
     if (st == DIAQ_OK) {
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) st = cuda_status(e, "cudaStreamSynchronize", __FILE__, __LINE__);
@@ -275,6 +287,7 @@ int copy_as(const Matrix &A, int prec, cudaStream_t s, Matrix **out) {
 }
 
 int prune_matrix(const Matrix &A, cudaStream_t s, Matrix **out) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "prune: convert a c128f2 matrix to c128 first");
     std::vector<int32_t> flag(A.nd, 1);
     if (A.nd > 0) {
         int32_t *d_flag = nullptr;

@@ -53,6 +53,14 @@ __global__ void pauli_fill_kernel(const DiagMeta *__restrict__ meta, int nd, con
 int pauli_build(int nq, int32_t ns, const double *cre, const double *cim, const uint64_t *xm, const uint64_t *zm,
                 int prec, cudaStream_t s, Matrix **out) {
     if (nq < 1 || nq > 30) return set_error(DIAQ_ERR_INVALID, "pauli: 1 <= n_qubits <= 30");
+    if (prec == DIAQ_C128F2) {  // built in float64, then split into float pairs
+        Matrix *D = nullptr;
+        DQ_TRY(pauli_build(nq, ns, cre, cim, xm, zm, DIAQ_C128, s, &D));
+        const int st = copy_as(*D, DIAQ_C128F2, s, out);
+        cudaStreamSynchronize(s);
+        destroy(D);
+        return st;
+    }
     if (ns < 0 || (ns > 0 && (!cre || !xm || !zm))) return set_error(DIAQ_ERR_INVALID, "pauli: NULL string arrays");
     const int64_t N = int64_t(1) << nq;
     const uint64_t full = (uint64_t)N - 1;

@@ -103,6 +103,7 @@ __global__ void compact_kernel(const uint8_t *__restrict__ flags, int64_t n, int
 
 // Symbolic phase on the device: result offsets (ascending, distinct) to the host vector.
 int spgemm_symbolic(const Matrix &A, const Matrix &B, std::vector<int32_t> &offC, cudaStream_t s) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "product: convert a c128f2 matrix to c128 first");
     offC.clear();
     if (A.cols != B.rows) return set_error(DIAQ_ERR_INVALID, "diaQMatrix product_cuda: dimension mismatch.");
     if (A.nd == 0 || B.nd == 0 || A.rows == 0 || B.cols == 0) return DIAQ_OK;
@@ -231,6 +232,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
 }
 
 int spgemm_numeric(const Matrix &A, const Matrix &B, Matrix &C, cudaStream_t s) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "product: convert a c128f2 matrix to c128 first");
     if (A.cols != B.rows || C.rows != A.rows || C.cols != B.cols)
         return set_error(DIAQ_ERR_INVALID, "diaQMatrix product_cuda: dimension mismatch.");
     if (A.prec != B.prec || A.prec != C.prec)
@@ -267,6 +269,7 @@ int spgemm_numeric(const Matrix &A, const Matrix &B, Matrix &C, cudaStream_t s) 
 }
 
 int spgemm(const Matrix &A, const Matrix &B, bool prune, cudaStream_t s, Matrix **out) {
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "product: convert a c128f2 matrix to c128 first");
     if (A.cols != B.rows) return set_error(DIAQ_ERR_INVALID, "diaQMatrix product_cuda: dimension mismatch.");
     if (A.prec != B.prec) return set_error(DIAQ_ERR_INVALID, "product: operands must have the same precision");
     std::vector<int32_t> offC;

@@ -12,6 +12,12 @@ int spmv_launch(const Matrix &A, const void *xr, const void *xi, int64_t ldx, vo
     if (!xr || !xi || !yr || !yi) return set_error(DIAQ_ERR_INVALID, "vector pointer is NULL");
     if (nrhs > 1 && (ldx < A.cols || ldy < A.rows))
         return set_error(DIAQ_ERR_INVALID, "leading dimension smaller than the vector length");
+    if (A.prec == DIAQ_C128F2) {  // float64 vectors, float-pair arithmetic; one state per launch
+        for (int q = 0; q < nrhs; ++q)
+            DQ_TRY(f2_spmv(A, (const double *)xr + q * ldx, (const double *)xi + q * ldx, (double *)yr + q * ldy,
+                           (double *)yi + q * ldy, s));
+        return DIAQ_OK;
+    }
     if (A.prec == DIAQ_C128) {
         EpiStoreRhs<double> e;
         e.yr = (double *)yr;
@@ -62,7 +68,8 @@ extern "C" {
 int diaq_spmv_z(diaq_matrix_t A, const double *x_re, const double *x_im, double *y_re,
                 double *y_im, void *stream) {
     if (!A) return set_error(DIAQ_ERR_INVALID, "matrix handle is NULL");
-    if (A->prec != DIAQ_C128) return set_error(DIAQ_ERR_INVALID, "diaq_spmv_z needs a c128 matrix");
+    if (A->prec != DIAQ_C128 && A->prec != DIAQ_C128F2)
+        return set_error(DIAQ_ERR_INVALID, "diaq_spmv_z needs a c128 or c128f2 matrix");
     return spmv_launch(*A, x_re, x_im, A->cols, y_re, y_im, A->rows, 1, (cudaStream_t)stream);
 }
 
@@ -97,7 +104,7 @@ extern "C" {
 int diaq_spmv_host(diaq_matrix_t A, const double *x_re, const double *x_im, double *y_re,
                    double *y_im) {
     if (!A) return set_error(DIAQ_ERR_INVALID, "matrix handle is NULL");
-    if (A->prec != DIAQ_C128) return set_error(DIAQ_ERR_INVALID, "spmv_cuda: needs a c128 matrix");
+    if (A->prec != DIAQ_C128 && A->prec != DIAQ_C128F2) return set_error(DIAQ_ERR_INVALID, "spmv_cuda: needs a c128 matrix");
     if (A->rows == 0) return DIAQ_OK;
     if (!x_re || !x_im || !y_re || !y_im) return set_error(DIAQ_ERR_INVALID, "vector pointer is NULL");
     Scratch w;

@@ -1,0 +1,260 @@
+// Complex128 SpMV on the FP32 pipes: DIAQ_C128F2 matrices.
+//
+// GB300 issues FP64 fused multiply-adds at 1/58 of its FP32 rate (0.59 vs 34.6 T/s measured),
+// so the float64 SpMV (4 DFMA per stored value) tops out near 2.4 TB/s of matrix traffic -- FP64
+// issue, not HBM, bounds it.  A DIAQ_C128F2 matrix keeps 16 bytes per complex value, but each
+// float64 v as a pair of floats hi = fl32(v), lo = fl32(v - hi) (a 48-bit significand), and the
+// kernel accumulates products of such pairs exactly enough on the FP32 pipes:
+//   product   p = ah*xh (+ error fma(ah, xh, -p)) + ah*xl + al*xh          (Dekker/Knuth with FMA)
+//   sum       (sh, sl) <- TwoSum(sh, p) with the error and the low parts added to sl
+// About 12 FP32 instructions per real product-accumulate, 48 per complex value: ~0.7 T complex
+// values/s, above the ~0.42 T/s at which HBM delivers the 16-byte values -- the kernel becomes
+// memory-bound.  Relative error ~1e-14 (2^-48 per value plus accumulation): inside the 1e-12 of
+// the float64 path's parity bar.  Range: magnitudes in roughly [1e-30, 1e38] keep the full
+// precision (the low float must stay normal).
+//
+// x arrives as float64 and is split once per call (one pass over N values); y is written as
+// float64 (hi + lo in double, 2 conversions and 1 add per row).
+//
+// Storage: the layout of the other precisions, the re (im) array holding the hi plane of
+// `capacity` floats followed by the lo plane.
+#include <algorithm>
+
+#include "spmv_kernel.cuh"
+
+namespace diaq_gb300 {
+
+__device__ __forceinline__ void split64(double v, float &h, float &l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+// packed float64 -> hi/lo planes
+__global__ void f2_scatter_kernel(const DiagMeta *__restrict__ meta, int nd, const double *__restrict__ sre,
+                                  const double *__restrict__ sim, float *__restrict__ re, float *__restrict__ im,
+                                  int64_t cap) {
+    for (int k = blockIdx.y; k < nd; k += gridDim.y) {
+        const DiagMeta m = meta[k];
+        const int64_t len = m.hi - m.lo;
+        for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < len; j += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t d = m.base + m.lo + j;
+            split64(sre[m.pstart + j], re[d], re[cap + d]);
+            split64(sim[m.pstart + j], im[d], im[cap + d]);
+        }
+    }
+}
+
+// hi/lo planes -> packed float64
+__global__ void f2_gather_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ re,
+                                 const float *__restrict__ im, int64_t cap, double *__restrict__ dre,
+                                 double *__restrict__ dim) {
+    for (int k = blockIdx.y; k < nd; k += gridDim.y) {
+        const DiagMeta m = meta[k];
+        const int64_t len = m.hi - m.lo;
+        for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < len; j += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t s = m.base + m.lo + j;
+            dre[m.pstart + j] = (double)re[s] + (double)re[cap + s];
+            dim[m.pstart + j] = (double)im[s] + (double)im[cap + s];
+        }
+    }
+}
+
+// float64 vector(s) -> hi/lo planes (n values each; planes of n)
+__global__ void f2_split_vec_kernel(const double *__restrict__ a, float *__restrict__ h, float *__restrict__ l, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        split64(a[i], h[i], l[i]);
+}
+
+struct F2 {
+    float h, l;
+};
+
+// s += a*x for float pairs (see the file comment); sign = -1 subtracts.
+__device__ __forceinline__ void f2_mac(F2 &s, float ah, float al, float xh, float xl, float sign) {
+    const float ph = (sign * ah) * xh;
+    float pl = fmaf(sign * ah, xh, -ph);
+    pl = fmaf(sign * ah, xl, pl);
+    pl = fmaf(sign * al, xh, pl);
+    const float t = s.h + ph;
+    const float bb = t - s.h;
+    const float e = (s.h - (t - bb)) + (ph - bb);
+    s.h = t;
+    s.l += e + pl;
+}
+
+// y = A x: each thread owns VR = 4 consecutive rows; hi and lo planes are separate SoA arrays, so
+// every matrix load is a 16-byte vector of 4 rows.  Strips that lie inside a diagonal read the
+// four x planes as aligned vectors shifted across lanes (the x planes are this file's scratch,
+// padded to a multiple of 32 values, so the aligned vectors stay inside them; values past column
+// cols are read but never used).  PF > 0 also prefetches the warp's 128-row strip of the four
+// matrix planes into L2 PF diagonals ahead; on the 20-qubit XXZ chain that measured slower
+// (216 vs 194 us), so the entry point runs PF = 0.
+
+__device__ __forceinline__ void f2_prefetch_strip(const DiagMeta &m, int64_t w0, const float *are,
+                                                  const float *aim, int64_t cap) {
+    const int64_t a = w0 > (m.lo & ~int64_t(31)) ? w0 : (m.lo & ~int64_t(31));
+    const int64_t hi32 = (m.hi + 31) & ~int64_t(31);
+    const int64_t b = (w0 + 128) < hi32 ? (w0 + 128) : hi32;
+    if (a >= b) return;
+    const unsigned bytes = (unsigned)(b - a) * 4u;
+    prefetch_l2_bulk(are + m.base + a, bytes);
+    prefetch_l2_bulk(are + cap + m.base + a, bytes);
+    prefetch_l2_bulk(aim + m.base + a, bytes);
+    prefetch_l2_bulk(aim + cap + m.base + a, bytes);
+}
+
+template <int PF>
+__global__ void __launch_bounds__(kSpmvThreads)
+    f2_spmv_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
+                   const float *__restrict__ aim, int64_t cap, int64_t rows, const float *__restrict__ xrh,
+                   const float *__restrict__ xrl, const float *__restrict__ xih, const float *__restrict__ xil,
+                   double *__restrict__ yr, double *__restrict__ yi) {
+    constexpr int V = 4;
+    __shared__ DiagMeta sm[kMetaChunk];
+    const int lane = threadIdx.x & 31;
+    const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
+    const int64_t w0 = r0 - (int64_t)V * lane;
+    F2 sr[V], si[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) sr[v] = si[v] = F2{0.f, 0.f};
+    for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
+        const int cn = min(kMetaChunk, nd - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
+        __syncthreads();
+        if (w0 >= rows) continue;
+        if (PF > 0 && lane == 0)
+            for (int k = 0; k < PF && k < cn; ++k) f2_prefetch_strip(sm[k], w0, are, aim, cap);
+        for (int k = 0; k < cn; ++k) {
+            if (PF > 0 && lane == 0 && k + PF < cn) f2_prefetch_strip(sm[k + PF], w0, are, aim, cap);
+            const int64_t lo = sm[k].lo, hi = sm[k].hi;
+            if (w0 >= hi || w0 + 32 * V <= lo) continue;  // the same for the whole warp
+            const int64_t b = sm[k].base + r0, c = r0 + sm[k].off;
+            float arh[V], arl[V], aih[V], ail[V];
+            float xrhv[V], xrlv[V], xihv[V], xilv[V];
+            if (w0 >= lo && w0 + 32 * V <= hi) {
+                load_vec_stream<float, V>(arh, are + b);
+                load_vec_stream<float, V>(arl, are + cap + b);
+                load_vec_stream<float, V>(aih, aim + b);
+                load_vec_stream<float, V>(ail, aim + cap + b);
+                const int s = (int)(c & 3);
+                const int64_t ca = c - s;
+                shifted_window(xrhv, xrh + ca, s, lane);
+                shifted_window(xrlv, xrl + ca, s, lane);
+                shifted_window(xihv, xih + ca, s, lane);
+                shifted_window(xilv, xil + ca, s, lane);
+            } else {
+                if (r0 >= rows || r0 + V <= lo || r0 >= hi) continue;
+                load_vec_stream<float, V>(arh, are + b);
+                load_vec_stream<float, V>(arl, are + cap + b);
+                load_vec_stream<float, V>(aih, aim + b);
+                load_vec_stream<float, V>(ail, aim + cap + b);
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    const bool ok = (r0 + v >= lo) && (r0 + v < hi);
+                    xrhv[v] = ok ? __ldg(xrh + c + v) : 0.f;
+                    xrlv[v] = ok ? __ldg(xrl + c + v) : 0.f;
+                    xihv[v] = ok ? __ldg(xih + c + v) : 0.f;
+                    xilv[v] = ok ? __ldg(xil + c + v) : 0.f;
+                    if (!ok) arh[v] = arl[v] = aih[v] = ail[v] = 0.f;
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                f2_mac(sr[v], arh[v], arl[v], xrhv[v], xrlv[v], 1.f);
+                f2_mac(sr[v], aih[v], ail[v], xihv[v], xilv[v], -1.f);
+                f2_mac(si[v], arh[v], arl[v], xihv[v], xilv[v], 1.f);
+                f2_mac(si[v], aih[v], ail[v], xrhv[v], xrlv[v], 1.f);
+            }
+        }
+    }
+    if (r0 >= rows) return;
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+        if (r0 + v < rows) {
+            yr[r0 + v] = (double)sr[v].h + (double)sr[v].l;
+            yi[r0 + v] = (double)si[v].h + (double)si[v].l;
+        }
+}
+
+__global__ void f2_from_c128_kernel(const DiagMeta *__restrict__ meta, int nd, const double *__restrict__ sre,
+                                    const double *__restrict__ sim, float *__restrict__ re, float *__restrict__ im,
+                                    int64_t cap) {
+    for (int k = blockIdx.y; k < nd; k += gridDim.y) {
+        const DiagMeta m = meta[k];
+        for (int64_t r = m.lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m.hi; r += (int64_t)gridDim.x * blockDim.x) {
+            split64(sre[m.base + r], re[m.base + r], re[cap + m.base + r]);
+            split64(sim[m.base + r], im[m.base + r], im[cap + m.base + r]);
+        }
+    }
+}
+
+__global__ void c128_from_f2_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ re,
+                                    const float *__restrict__ im, int64_t cap, double *__restrict__ dre,
+                                    double *__restrict__ dim) {
+    for (int k = blockIdx.y; k < nd; k += gridDim.y) {
+        const DiagMeta m = meta[k];
+        for (int64_t r = m.lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m.hi; r += (int64_t)gridDim.x * blockDim.x) {
+            dre[m.base + r] = (double)re[m.base + r] + (double)re[cap + m.base + r];
+            dim[m.base + r] = (double)im[m.base + r] + (double)im[cap + m.base + r];
+        }
+    }
+}
+
+static dim3 f2_grid(const Matrix &M) {
+    int64_t maxlen = 1;
+    for (const auto &m : M.meta) maxlen = std::max(maxlen, m.hi - m.lo);
+    return dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>((maxlen + 1023) / 1024, 4 * num_sms())),
+                (unsigned)std::min<int64_t>(std::max<int32_t>(M.nd, 1), 65535));
+}
+
+int f2_scatter(Matrix &M, const double *re, const double *im, cudaStream_t s) {
+    if (M.nd == 0) return DIAQ_OK;
+    f2_scatter_kernel<<<f2_grid(M), 256, 0, s>>>(M.d_meta, M.nd, re, im, (float *)M.re, (float *)M.im, M.capacity);
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
+}
+
+int f2_gather(const Matrix &M, double *re, double *im, cudaStream_t s) {
+    if (M.nd == 0) return DIAQ_OK;
+    f2_gather_kernel<<<f2_grid(M), 256, 0, s>>>(M.d_meta, M.nd, (const float *)M.re, (const float *)M.im, M.capacity, re,
+                                                im);
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
+}
+
+// Same offsets and layout (src and dst planned alike); one precision is C128, the other C128F2.
+int f2_convert(const Matrix &src, Matrix &dst, cudaStream_t s) {
+    if (dst.nd == 0) return DIAQ_OK;
+    if (src.prec == DIAQ_C128 && dst.prec == DIAQ_C128F2)
+        f2_from_c128_kernel<<<f2_grid(dst), 256, 0, s>>>(src.d_meta, src.nd, (const double *)src.re, (const double *)src.im,
+                                                        (float *)dst.re, (float *)dst.im, dst.capacity);
+    else if (src.prec == DIAQ_C128F2 && dst.prec == DIAQ_C128)
+        c128_from_f2_kernel<<<f2_grid(dst), 256, 0, s>>>(src.d_meta, src.nd, (const float *)src.re, (const float *)src.im,
+                                                        src.capacity, (double *)dst.re, (double *)dst.im);
+    else
+        return set_error(DIAQ_ERR_UNSUPPORTED, "c128f2 matrices convert to and from c128 only");
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
+}
+
+int f2_spmv(const Matrix &A, const double *xr, const double *xi, double *yr, double *yi, cudaStream_t s) {
+    if (A.rows == 0) return DIAQ_OK;
+    const int64_t n = A.cols;
+    const int64_t np = (n + 31) / 32 * 32;  // planes 128-byte aligned: equal alignment for hi and lo
+    float *buf = nullptr;
+    DQ_CUDA(cudaMallocAsync(&buf, sizeof(float) * 4 * (size_t)std::max<int64_t>(np, 32), s));
+    float *xrh = buf, *xrl = buf + np, *xih = buf + 2 * np, *xil = buf + 3 * np;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * num_sms()));
+    f2_split_vec_kernel<<<g, 256, 0, s>>>(xr, xrh, xrl, n);
+    f2_split_vec_kernel<<<g, 256, 0, s>>>(xi, xih, xil, n);
+    f2_spmv_kernel<0><<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
+                                                                  (const float *)A.im, A.capacity, A.rows, xrh, xrl,
+                                                                  xih, xil, yr, yi);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(buf, s);
+    if (e != cudaSuccess) return cuda_status(e, "f2 spmv", __FILE__, __LINE__);
+    return DIAQ_OK;
+}
+
+}  // namespace diaq_gb300

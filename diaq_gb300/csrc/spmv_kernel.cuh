@@ -85,16 +85,26 @@ __device__ __forceinline__ bool aligned_to(const void *p) {
 }
 __device__ __forceinline__ bool aligned16(const void *p) { return aligned_to<16>(p); }
 
-// K states (kq of them live), VR rows per thread.
+// nrhs states in nchunk chunks of up to K, VR rows per thread.  Block b works on chunk
+// b % nchunk of row tile b / nchunk: the blocks of one row tile are neighbours in launch order and
+// run at the same time, so the matrix tile they all read comes from HBM once and from L2 for the
+// other chunks -- the matrix traffic of one launch over all states, with the registers of K.
 template <typename T, int K, int VR, class Epi>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_kernel(const DiagMeta *__restrict__ meta, int nd, const T *__restrict__ are,
                     const T *__restrict__ aim, int64_t rows, const T *__restrict__ xr,
-                    const T *__restrict__ xi, int64_t ldx, int kq, Epi epi) {
+                    const T *__restrict__ xi, int64_t ldx, int nrhs, int nchunk, Epi epi0) {
     constexpr int V = VR;
     constexpr int VB = VR * (int)sizeof(T);
     __shared__ DiagMeta sm[kMetaChunk];
-    const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
+    const int chunk = (int)(blockIdx.x % (unsigned)nchunk);
+    const int64_t tile = blockIdx.x / (unsigned)nchunk;
+    const int q0 = chunk * K;
+    const int kq = min(K, nrhs - q0);
+    xr += q0 * ldx;
+    xi += q0 * ldx;
+    const Epi epi = epi0.shifted(q0);
+    const int64_t r0 = (tile * kSpmvThreads + threadIdx.x) * V;
     T accr[K][V], acci[K][V];
 #pragma unroll
     for (int q = 0; q < K; ++q)
@@ -151,6 +161,171 @@ __global__ void __launch_bounds__(kSpmvThreads)
         }
     }
     if (r0 < rows) epi.template apply<T, K, V>(r0, rows, kq, accr, acci);
+}
+
+// ---- float variant with L2 prefetch of the matrix and shuffled state windows ----------------------
+//
+// The register kernel above waits, on every diagonal, for the HBM latency of its matrix vector:
+// a warp has one diagonal's loads in flight, and a few dozen warps per SM do not cover the
+// latency (profiles: ~30 % of HBM bandwidth, long-scoreboard stalls).  Here lane 0 of each warp
+// asks L2 for the warp's 128-row strip of the matrix PF diagonals ahead with one bulk prefetch
+// per array (cp.async.bulk.prefetch.L2: no registers, no shared memory), so the loads the warp
+// then issues hit L2.
+//
+// The state windows of a diagonal whose offset is not a multiple of 4 start between 16-byte
+// vectors.  The offset is the same for the whole warp, so each lane loads its aligned vector
+// and takes the next one from the neighbouring lane (lane 31 loads it): one 16-byte load per
+// lane instead of four 4-byte loads.  Strips that a diagonal covers only in part (at the
+// matrix's edges) take the element-wise path of the register kernel.
+//
+// Needs cols % 4 == 0, ldx % 4 == 0 and 16-byte aligned x arrays (checked by the launcher);
+// then every x read stays below column cols.
+
+// Ask L2 for [p, p + bytes): p 16-byte aligned, bytes a multiple of 16.  The lines come in with
+// evict-first priority, like the streaming loads that will read them, so that they do not push
+// the re-read state windows out of L2.
+__device__ __forceinline__ void prefetch_l2_bulk(const void *p, unsigned bytes) {
+    uint64_t policy;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(policy));
+    asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;\n" ::"l"(p), "r"(bytes), "l"(policy)
+                 : "memory");
+}
+
+// Rows [w0, w0 + 128) of diagonal m, clipped to the diagonal's rows rounded out to 32 values
+// (inside the allocation: the first diagonal starts 32 values in and 32 values follow the last;
+// base is a multiple of 32, so the clipped range starts on a 128-byte boundary).
+__device__ __forceinline__ void prefetch_strip(const DiagMeta &m, int64_t w0, const float *are,
+                                               const float *aim) {
+    const int64_t a = w0 > (m.lo & ~int64_t(31)) ? w0 : (m.lo & ~int64_t(31));
+    const int64_t hi32 = (m.hi + 31) & ~int64_t(31);
+    const int64_t b = (w0 + 128) < hi32 ? (w0 + 128) : hi32;
+    if (a >= b) return;
+    prefetch_l2_bulk(are + m.base + a, (unsigned)(b - a) * 4u);
+    prefetch_l2_bulk(aim + m.base + a, (unsigned)(b - a) * 4u);
+}
+
+// The four values x[c .. c+3] for a warp whose lanes own consecutive 4-row groups, c - s the
+// lane's aligned vector (s = c & 3, the same in every lane).
+__device__ __forceinline__ void shifted_window(float (&out)[4], const float *aligned_p, int s, int lane) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(aligned_p));
+    if (s == 0) {
+        out[0] = a.x;
+        out[1] = a.y;
+        out[2] = a.z;
+        out[3] = a.w;
+        return;
+    }
+    float n0 = __shfl_down_sync(0xffffffffu, a.x, 1);
+    float n1 = __shfl_down_sync(0xffffffffu, a.y, 1);
+    float n2 = __shfl_down_sync(0xffffffffu, a.z, 1);
+    if (lane == 31) {
+        const float4 b = __ldg(reinterpret_cast<const float4 *>(aligned_p + 4));
+        n0 = b.x;
+        n1 = b.y;
+        n2 = b.z;
+    }
+    if (s == 1) {
+        out[0] = a.y;
+        out[1] = a.z;
+        out[2] = a.w;
+        out[3] = n0;
+    } else if (s == 2) {
+        out[0] = a.z;
+        out[1] = a.w;
+        out[2] = n0;
+        out[3] = n1;
+    } else {
+        out[0] = a.w;
+        out[1] = n0;
+        out[2] = n1;
+        out[3] = n2;
+    }
+}
+
+template <int K, int PF, class Epi>
+__global__ void __launch_bounds__(kSpmvThreads)
+    dia_spmv_pf_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
+                       const float *__restrict__ aim, int64_t rows, const float *__restrict__ xr,
+                       const float *__restrict__ xi, int64_t ldx, int kq, Epi epi) {
+    constexpr int V = 4;
+    __shared__ DiagMeta sm[kMetaChunk];
+    const int lane = threadIdx.x & 31;
+    const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
+    const int64_t w0 = r0 - (int64_t)V * lane;  // first row of the warp's 128-row strip
+    float accr[K][V], acci[K][V];
+#pragma unroll
+    for (int q = 0; q < K; ++q)
+#pragma unroll
+        for (int v = 0; v < V; ++v) accr[q][v] = acci[q][v] = 0.f;
+
+    for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
+        const int cn = min(kMetaChunk, nd - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
+        __syncthreads();
+        if (w0 >= rows) continue;  // the whole warp is past the last row
+        if (PF > 0 && lane == 0)
+            for (int k = 0; k < PF && k < cn; ++k) prefetch_strip(sm[k], w0, are, aim);
+        for (int k = 0; k < cn; ++k) {
+            if (PF > 0 && lane == 0 && k + PF < cn) prefetch_strip(sm[k + PF], w0, are, aim);
+            const int64_t lo = sm[k].lo, hi = sm[k].hi;
+            if (w0 >= hi || w0 + 32 * V <= lo) continue;  // the same for the whole warp
+            const int64_t base = sm[k].base;
+            const int64_t c = r0 + sm[k].off;
+            if (w0 >= lo && w0 + 32 * V <= hi) {
+                // the strip lies inside the diagonal: every lane has 4 valid rows
+                float ar[V], ai[V];
+                load_vec_stream<float, V>(ar, are + base + r0);
+                load_vec_stream<float, V>(ai, aim + base + r0);
+                const int s = (int)(c & 3);
+                const int64_t ca = c - s;
+#pragma unroll
+                for (int q = 0; q < K; ++q) {
+                    if (q >= kq) break;
+                    float xrv[V], xiv[V];
+                    shifted_window(xrv, xr + q * ldx + ca, s, lane);
+                    shifted_window(xiv, xi + q * ldx + ca, s, lane);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) {
+                        accr[q][v] = fmaf(ar[v], xrv[v], accr[q][v]);
+                        accr[q][v] = fmaf(-ai[v], xiv[v], accr[q][v]);
+                        acci[q][v] = fmaf(ar[v], xiv[v], acci[q][v]);
+                        acci[q][v] = fmaf(ai[v], xrv[v], acci[q][v]);
+                    }
+                }
+            } else {
+                // edge strip: element-wise, rows outside [lo, hi) (and past the last row) masked
+                if (r0 >= rows || r0 + V <= lo || r0 >= hi) continue;
+                float ar[V], ai[V];
+                load_vec_stream<float, V>(ar, are + base + r0);
+                load_vec_stream<float, V>(ai, aim + base + r0);
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    if (r0 + v < lo || r0 + v >= hi) ar[v] = ai[v] = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; ++q) {
+                    if (q >= kq) break;
+                    const float *pxr = xr + q * ldx + c, *pxi = xi + q * ldx + c;
+#pragma unroll
+                    for (int v = 0; v < V; ++v) {
+                        const bool ok = (r0 + v >= lo) && (r0 + v < hi);
+                        const float xv = ok ? __ldg(pxr + v) : 0.f, yv = ok ? __ldg(pxi + v) : 0.f;
+                        accr[q][v] = fmaf(ar[v], xv, accr[q][v]);
+                        accr[q][v] = fmaf(-ai[v], yv, accr[q][v]);
+                        acci[q][v] = fmaf(ar[v], yv, acci[q][v]);
+                        acci[q][v] = fmaf(ai[v], xv, acci[q][v]);
+                    }
+                }
+            }
+        }
+    }
+    if (r0 < rows) epi.template apply<float, K, V>(r0, rows, kq, accr, acci);
+}
+
+// Whether the prefetching kernel may run on these state arrays (see its notes).
+inline bool pf_kernel_fits(const Matrix &A, const float *xr, const float *xi, int64_t ldx, int nrhs) {
+    return A.cols % 4 == 0 && (nrhs == 1 || ldx % 4 == 0) && (reinterpret_cast<uintptr_t>(xr) & 15) == 0 &&
+           (reinterpret_cast<uintptr_t>(xi) & 15) == 0;
 }
 
 // Store y = A x.
@@ -237,47 +412,91 @@ inline unsigned spmv_blocks(int64_t rows, int V) {
 struct SpmvCfg {
     int kmax = 8;
     int vr = 0;
-    int pipe = 0;  // 1: the cp.async-pipelined float kernel (4 rows per thread)
+    int pipe = 0;  // float kernels, 4 rows per thread: 1 cp.async pipeline; shuffled windows with L2 prefetch
+                   // 4 (2) or 8 (3) diagonals ahead, or without prefetch (4)
 };
 
 template <typename T, int K, class Epi, int VR, int... More>
-void launch_vr(int vr, const Matrix &A, const T *xr, const T *xi, int64_t ldx, int kq, const Epi &e,
+void launch_vr(int vr, const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, int nchunk, const Epi &e,
                cudaStream_t s) {
     if constexpr (sizeof...(More) > 0) {
         if (vr != VR) {
-            launch_vr<T, K, Epi, More...>(vr, A, xr, xi, ldx, kq, e, s);
+            launch_vr<T, K, Epi, More...>(vr, A, xr, xi, ldx, nrhs, nchunk, e, s);
             return;
         }
     }
-    dia_spmv_kernel<T, K, VR, Epi><<<spmv_blocks(A.rows, VR), kSpmvThreads, 0, s>>>(
-        A.d_meta, A.nd, (const T *)A.re, (const T *)A.im, A.rows, xr, xi, ldx, kq, e);
+    dia_spmv_kernel<T, K, VR, Epi><<<spmv_blocks(A.rows, VR) * (unsigned)nchunk, kSpmvThreads, 0, s>>>(
+        A.d_meta, A.nd, (const T *)A.re, (const T *)A.im, A.rows, xr, xi, ldx, nrhs, nchunk, e);
 }
 
-// Launch over the right-hand sides in chunks of up to cfg.kmax (<= 8; one matrix read per chunk,
-// the kernel instantiated for 1, 2, 4 or 8 states with the unused slots masked).  VRs lists the
-// rows-per-thread variants compiled for this epilogue (the first is the default).  Epi must
-// offer `shifted(q0)`, the same epilogue for right-hand sides q0.. .
+// One launch over all right-hand sides, in chunks of up to cfg.kmax (<= 8) states per block
+// (the kernel instantiated for 1, 2, 4 or 8 states, unused slots of the last chunk masked); the
+// chunks of a row tile run side by side (see dia_spmv_kernel).  VRs lists the rows-per-thread
+// variants compiled for this epilogue (the first is the default).  Epi must offer
+// `shifted(q0)` on host and device, the same epilogue for right-hand sides q0.. .
 template <typename T, class Epi, int... VRs>
 int launch_dia_spmv_rhs_cfg(const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, Epi epi,
                             cudaStream_t s, SpmvCfg cfg) {
     if (A.rows == 0 || nrhs <= 0) return DIAQ_OK;
-    const int kmax = cfg.kmax >= 8 ? 8 : cfg.kmax >= 4 ? 4 : cfg.kmax >= 2 ? 2 : 1;
+    int k = cfg.kmax >= 8 ? 8 : cfg.kmax >= 4 ? 4 : cfg.kmax >= 2 ? 2 : 1;
+    while (k > 1 && k / 2 >= nrhs) k /= 2;  // no wider than the states need
     const int vr = cfg.vr > 0 ? cfg.vr : VecOf<T>::V;
+    const int nchunk = (nrhs + k - 1) / k;
+    if ((uint64_t)spmv_blocks(A.rows, vr) * (uint64_t)nchunk > 0x7fffffffull)
+        return set_error(DIAQ_ERR_UNSUPPORTED, "spmv: too many row tiles x state chunks for one launch");
+    if (k == 8)
+        launch_vr<T, 8, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s);
+    else if (k == 4)
+        launch_vr<T, 4, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s);
+    else if (k == 2)
+        launch_vr<T, 2, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s);
+    else
+        launch_vr<T, 1, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s);
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
+}
+
+// The shuffled-window float kernel over the states in chunks of up to kmax; variant 2 / 3
+// prefetches the matrix 4 / 8 diagonals ahead, variant 4 does not prefetch.  Falls back to the
+// register kernel (4 rows per thread) where pf_kernel_fits does not hold.
+template <int K, class Epi>
+void launch_pf_k(int variant, const Matrix &A, const float *xr, const float *xi, int64_t ldx, int kq, const Epi &e,
+                 cudaStream_t s) {
+    const unsigned g = spmv_blocks(A.rows, 4);
+    const float *are = (const float *)A.re, *aim = (const float *)A.im;
+    if (variant == 3)
+        dia_spmv_pf_kernel<K, 8, Epi><<<g, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, are, aim, A.rows, xr, xi, ldx, kq, e);
+    else if (variant == 4)
+        dia_spmv_pf_kernel<K, 0, Epi><<<g, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, are, aim, A.rows, xr, xi, ldx, kq, e);
+    else
+        dia_spmv_pf_kernel<K, 4, Epi><<<g, kSpmvThreads, 0, s>>>(A.d_meta, A.nd, are, aim, A.rows, xr, xi, ldx, kq, e);
+}
+
+template <class Epi>
+int launch_dia_spmv_pf(const Matrix &A, const float *xr, const float *xi, int64_t ldx, int nrhs, Epi epi,
+                       cudaStream_t s, int kmax, int variant, int *launches) {
+    if (A.rows == 0 || nrhs <= 0) return DIAQ_OK;
+    if (!pf_kernel_fits(A, xr, xi, ldx, nrhs)) {
+        ++*launches;
+        return launch_dia_spmv_rhs_cfg<float, Epi, 4>(A, xr, xi, ldx, nrhs, epi, s, SpmvCfg{kmax, 4, 0});
+    }
+    kmax = kmax >= 8 ? 8 : kmax >= 4 ? 4 : kmax >= 2 ? 2 : 1;
     int q0 = 0;
     while (q0 < nrhs) {
         const int left = nrhs - q0;
         const int kq = left < kmax ? left : kmax;
-        const T *pxr = xr + q0 * ldx, *pxi = xi + q0 * ldx;
+        const float *pxr = xr + q0 * ldx, *pxi = xi + q0 * ldx;
         const Epi e = epi.shifted(q0);
         if (kq > 4)
-            launch_vr<T, 8, Epi, VRs...>(vr, A, pxr, pxi, ldx, kq, e, s);
+            launch_pf_k<8, Epi>(variant, A, pxr, pxi, ldx, kq, e, s);
         else if (kq > 2)
-            launch_vr<T, 4, Epi, VRs...>(vr, A, pxr, pxi, ldx, kq, e, s);
+            launch_pf_k<4, Epi>(variant, A, pxr, pxi, ldx, kq, e, s);
         else if (kq == 2)
-            launch_vr<T, 2, Epi, VRs...>(vr, A, pxr, pxi, ldx, kq, e, s);
+            launch_pf_k<2, Epi>(variant, A, pxr, pxi, ldx, kq, e, s);
         else
-            launch_vr<T, 1, Epi, VRs...>(vr, A, pxr, pxi, ldx, kq, e, s);
+            launch_pf_k<1, Epi>(variant, A, pxr, pxi, ldx, kq, e, s);
         q0 += kq;
+        ++*launches;
     }
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;
@@ -292,7 +511,7 @@ int launch_dia_spmv_rhs(const Matrix &A, const T *xr, const T *xi, int64_t ldx, 
 
 template <typename T>
 struct EpiStoreRhs : EpiStore<T> {
-    EpiStoreRhs shifted(int q0) const {
+    __host__ __device__ EpiStoreRhs shifted(int q0) const {
         EpiStoreRhs e = *this;
         e.yr += q0 * this->ldy;
         e.yi += q0 * this->ldy;
@@ -302,7 +521,7 @@ struct EpiStoreRhs : EpiStore<T> {
 
 template <typename T>
 struct EpiTaylorRhs : EpiTaylor<T> {
-    EpiTaylorRhs shifted(int q0) const {
+    __host__ __device__ EpiTaylorRhs shifted(int q0) const {
         EpiTaylorRhs e = *this;
         const int64_t o = q0 * this->ld;
         e.tr += o;

@@ -167,7 +167,7 @@ void launch_pipe_k(const Matrix &A, const float *xr, const float *xi, int64_t ld
 // The state windows must be float arrays with N values per state at leading dimension ldx.
 template <class Epi>
 int launch_dia_spmv_pipe(const Matrix &A, const float *xr, const float *xi, int64_t ldx, int nrhs, Epi epi,
-                         cudaStream_t s, int kmax) {
+                         cudaStream_t s, int kmax, int *launches) {
     if (A.rows == 0 || nrhs <= 0) return DIAQ_OK;
     kmax = kmax >= 8 ? 8 : kmax >= 4 ? 4 : kmax >= 2 ? 2 : 1;
     int q0 = 0;
@@ -185,6 +185,7 @@ int launch_dia_spmv_pipe(const Matrix &A, const float *xr, const float *xi, int6
         else
             launch_pipe_k<1, pipe_stages<1>(), Epi>(A, pxr, pxi, ldx, kq, e, s);
         q0 += kq;
+        ++*launches;
     }
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;

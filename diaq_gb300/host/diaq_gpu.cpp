@@ -176,7 +176,8 @@ DevPtr upload(const HostPtr &A, int prec = DIAQ_C128) { return std::make_shared<
 int parse_precision(const std::string &p) {
     if (p == "c128" || p == "complex128" || p == "fp64") return DIAQ_C128;
     if (p == "c64" || p == "complex64" || p == "fp32") return DIAQ_C64;
-    throw std::invalid_argument("precision must be 'c128' or 'c64'");
+    if (p == "c128f2") return DIAQ_C128F2;
+    throw std::invalid_argument("precision must be 'c128', 'c64' or 'c128f2'");
 }
 
 // ---- conversions (src/conversions.cpp, src/dense_to_diagonals.hpp:20-58) --------------------------
@@ -341,7 +342,7 @@ PYBIND11_MODULE(diaq_gpu, m) {
             int32_t nd;
             int p;
             d.info(r, c, nd, t, p);
-            return std::string(p == DIAQ_C128 ? "c128" : "c64");
+            return std::string(p == DIAQ_C128 ? "c128" : p == DIAQ_C64 ? "c64" : "c128f2");
         })
         .def_property_readonly("diagonals", &DeviceMatrix::diagonals)
         .def_property_readonly("handle", [](const DeviceMatrix &d) { return reinterpret_cast<uintptr_t>(d.h); });
@@ -409,7 +410,7 @@ PYBIND11_MODULE(diaq_gpu, m) {
             int32_t nd;
             int p;
             A->info(r, c, nd, t, p);
-            if (p == DIAQ_C128)
+            if (p != DIAQ_C64)
                 check(diaq_spmv_z(A->h, reinterpret_cast<const double *>(x_real), reinterpret_cast<const double *>(x_imag),
                                   reinterpret_cast<double *>(y_real), reinterpret_cast<double *>(y_imag),
                                   reinterpret_cast<void *>(stream)));
@@ -419,7 +420,7 @@ PYBIND11_MODULE(diaq_gpu, m) {
                                   reinterpret_cast<void *>(stream)));
         },
         py::arg("A"), py::arg("x_real"), py::arg("x_imag"), py::arg("y_real"), py::arg("y_imag"), py::arg("stream") = 0,
-        "y = A x with x, y as GPU arrays (float64 for a c128 matrix, float32 for c64; real and imaginary parts, e.g. "
+        "y = A x with x, y as GPU arrays (float64 for a c128 or c128f2 matrix, float32 for c64; real and imaginary parts, e.g. "
         "torch data pointers); y is overwritten; asynchronous on `stream`.");
     m.def(
         "spmm_device",
@@ -432,6 +433,19 @@ PYBIND11_MODULE(diaq_gpu, m) {
         py::arg("A"), py::arg("nrhs"), py::arg("x_real"), py::arg("x_imag"), py::arg("ldx"), py::arg("y_real"),
         py::arg("y_imag"), py::arg("ldy"), py::arg("stream") = 0,
         "Y = A X for nrhs right-hand sides stored one after another (leading dimensions ldx, ldy); asynchronous.");
+    // include/pythonWrappers.cpp:622-633
+    m.def(
+        "spmm_dia_device",
+        [](uintptr_t offsets, uintptr_t vals, int n_diags, int64_t n_rows, int64_t n_cols, uintptr_t B, int64_t n_right,
+           uintptr_t C, bool is_complex, uintptr_t stream) {
+            check(diaq_spmm_dia_device(reinterpret_cast<const int64_t *>(offsets), reinterpret_cast<const void *>(vals),
+                                       n_diags, n_rows, n_cols, reinterpret_cast<const void *>(B), n_right,
+                                       reinterpret_cast<void *>(C), is_complex ? 1 : 0, reinterpret_cast<void *>(stream)));
+        },
+        py::arg("offsets"), py::arg("vals"), py::arg("n_diags"), py::arg("n_rows"), py::arg("n_cols"), py::arg("B"),
+        py::arg("n_right"), py::arg("C"), py::arg("is_complex"), py::arg("stream") = 0,
+        "C = A * B, A in row-aligned DIA format (offsets int64[n_diags], vals[n_diags * n_rows]); B (n_cols x "
+        "n_right) and C (n_rows x n_right) row-major; double or complex double; all pointers on the GPU.");
 
     // ---- SpGEMM ----
     m.def("product", &product_host, "C = A B for host matrices; exact-zero result diagonals are pruned.");
@@ -529,7 +543,7 @@ PYBIND11_MODULE(diaq_gpu, m) {
         info["CUDA_ENABLED"] = true;
         info["GPU_ARCH"] = "sm_103a";
         info["valType"] = "double";
-        info["precisions"] = std::vector<std::string>{"c128", "c64"};
+        info["precisions"] = std::vector<std::string>{"c128", "c64", "c128f2"};
         info["version"] = std::string(diaq_version());
         return info;
     });

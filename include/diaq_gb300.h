@@ -37,8 +37,14 @@ typedef enum {
 } diaq_status;
 
 typedef enum {
-    DIAQ_C128 = 0, /* complex double, SoA float64 */
-    DIAQ_C64 = 1   /* complex float, SoA float32 */
+    DIAQ_C128 = 0,  /* complex double, SoA float64 */
+    DIAQ_C64 = 1,   /* complex float, SoA float32 */
+    DIAQ_C128F2 = 2 /* complex double held as float pairs (hi + lo, ~48-bit significand, 16 bytes
+                       per value) so that SpMV runs on the FP32 pipes: on GB300 FP64 issues at
+                       1/58 of the FP32 rate.  Relative error ~1e-14; magnitudes in about
+                       [1e-30, 1e38].  Supports create / download / copy / convert (to and from
+                       c128) and SpMV with float64 vectors (diaq_spmv_z, diaq_spmm,
+                       diaq_spmv_host); other operations return DIAQ_ERR_UNSUPPORTED. */
 } diaq_precision;
 
 typedef enum {
@@ -125,7 +131,8 @@ int diaq_spmm(diaq_matrix_t A, int nrhs, const void *x_re, const void *x_im, int
               void *y_re, void *y_im, int64_t ldy, void *stream);
 
 /* Host vectors in and out (x, y copied; A stays on the device).  Replaces
- * spmv_cuda(shared_ptr<deviceDiaQMatrix>, x) (src/spMV_gpu.cu:170-204).  c128 only.  Synchronous. */
+ * spmv_cuda(shared_ptr<deviceDiaQMatrix>, x) (src/spMV_gpu.cu:170-204).  c128 or c128f2 matrix.
+ * Synchronous. */
 int diaq_spmv_host(diaq_matrix_t A, const double *x_re, const double *x_im, double *y_re,
                    double *y_im);
 
@@ -134,6 +141,16 @@ int diaq_spmv_host(diaq_matrix_t A, const double *x_re, const double *x_im, doub
  * c128 only.  Synchronous. */
 int diaq_spmv_ntimes_host(diaq_matrix_t A, const double *x_re, const double *x_im, int n,
                           double *y_re, double *y_im);
+
+/* C = A B with A in the row-aligned DIA format and B, C dense, every array on the device:
+ * offsets int64[n_diags]; vals[k*n_rows + r] = A[r, r + offsets[k]] (entries whose column lies
+ * outside [0, n_cols) are ignored); B n_cols x n_right and C n_rows x n_right, row-major;
+ * float64 (is_complex = 0) or interleaved complex128 (is_complex != 0).  C is overwritten;
+ * diagonals are summed in the order given.  Asynchronous on stream.  Replaces spmm_dia_device
+ * (src/spMM_device_gpu.cu:113-127, bound at include/pythonWrappers.cpp:622-633). */
+int diaq_spmm_dia_device(const int64_t *offsets, const void *vals, int n_diags, int64_t n_rows,
+                         int64_t n_cols, const void *B, int64_t n_right, void *C, int is_complex,
+                         void *stream);
 
 /* ------------------------------------------------------------------------------------------
  * SpGEMM.  Replaces product_device / product_cuda (src/spGEMM_gpu.cu:84-161) and the host
@@ -217,7 +234,9 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
 
 /* Launch shape of the plan's term kernel: states per launch (1..8; the matrix is read once per
  * launch), rows per thread (1, 2, or 4 for the mixed mode) and, for the mixed mode with 4 rows,
- * pipelined != 0 to stream the next diagonals through shared memory with asynchronous copies.
+ * the kernel variant `pipelined`: 0 registers only, 1 stream the next diagonals through shared
+ * memory with asynchronous copies, 2 / 3 / 4 read unaligned state windows as aligned vectors
+ * shifted across lanes and prefetch the matrix into L2 4 / 8 / 0 diagonals ahead.
  * 0 states = choose automatically: on the first run the autotuner times the candidate shapes on
  * two steps of scratch copies of the states and keeps the fastest, caching the choice in a JSON
  * file (DIAQ_AUTOTUNE_CACHE, else $HOME/.cache/diaq_gb300/autotune.json).  Setting a shape drops

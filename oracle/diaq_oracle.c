@@ -267,6 +267,40 @@ void diaq_ham_sim(int64_t n, int32_t nd, const int32_t *off, const double *re, c
     free(buf);
 }
 
+/* ------------------------------------------------------------------------------------------
+ * DIA x dense, src/spMM_device_gpu.cu:44-127 (spmm_dia_device): C = A B with A in the row-aligned
+ * DIA format, vals[k*M + r] = A[r, r + off[k]] (columns outside [0, K) ignored), B K x R and C
+ * M x R row-major, float64 (is_complex = 0) or interleaved complex128.  Every element of C sums
+ * the diagonals in the order given (src/spMM_device_gpu.cu:60-74); C is overwritten.
+ * ---------------------------------------------------------------------------------------- */
+void diaq_spmm_dia(const int64_t *off, int32_t nd, int64_t M, int64_t K, const double *vals,
+                   const double *B, int64_t R, double *C, int32_t is_complex) {
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < M; ++r) {
+        for (int64_t j = 0; j < R; ++j) {
+            double ar = 0.0, ai = 0.0;
+            for (int32_t k = 0; k < nd; ++k) {
+                const int64_t c = r + off[k];
+                if (c < 0 || c >= K) continue;
+                if (is_complex) {
+                    const double vr = vals[2 * (k * M + r)], vi = vals[2 * (k * M + r) + 1];
+                    const double br = B[2 * (c * R + j)], bi = B[2 * (c * R + j) + 1];
+                    ar = ar + vr * br - vi * bi;
+                    ai = ai + vr * bi + vi * br;
+                } else {
+                    ar = ar + vals[k * M + r] * B[c * R + j];
+                }
+            }
+            if (is_complex) {
+                C[2 * (r * R + j)] = ar;
+                C[2 * (r * R + j) + 1] = ai;
+            } else {
+                C[r * R + j] = ar;
+            }
+        }
+    }
+}
+
 int diaq_oracle_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

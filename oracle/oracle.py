@@ -55,6 +55,7 @@ def lib():
         L.diaq_frobenius.restype = f64
         L.diaq_frobenius.argtypes = [i64, P, P]
         L.diaq_ham_sim.argtypes = [i64, i32, P, P, P, P, P, f64, i64, i32, i32, P, P]
+        L.diaq_spmm_dia.argtypes = [P, i32, i64, i64, P, P, i64, P, i32]
         L.diaq_oracle_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -151,6 +152,22 @@ def spmv(A: OMatrix, x: np.ndarray) -> np.ndarray:
     yr, yi = np.empty(A.rows), np.empty(A.rows)
     lib().diaq_spmv(A.rows, A.cols, A.nd, _p(A.off), _p(A.re), _p(A.im), _p(xr), _p(xi), _p(yr), _p(yi))
     return yr + 1j * yi
+
+
+def spmm_dia(offsets, vals: np.ndarray, n_cols: int, B: np.ndarray) -> np.ndarray:
+    """C = A B for A in the row-aligned DIA format (vals[k, r] = A[r, r + offsets[k]]), B dense
+    (n_cols x R), float64 or complex128 (src/spMM_device_gpu.cu:44-127)."""
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    cplx = np.iscomplexobj(vals) or np.iscomplexobj(B)
+    dt = np.complex128 if cplx else np.float64
+    V = np.ascontiguousarray(vals, dtype=dt)
+    Bm = np.ascontiguousarray(B, dtype=dt)
+    nd, M = V.shape
+    R = Bm.shape[1]
+    assert Bm.shape[0] == n_cols and len(off) == nd
+    C = np.empty((M, R), dtype=dt)
+    lib().diaq_spmm_dia(_p(off), nd, M, n_cols, _p(V), _p(Bm), R, _p(C), 1 if cplx else 0)
+    return C
 
 
 def spgemm_symbolic(A: OMatrix, B: OMatrix) -> np.ndarray:

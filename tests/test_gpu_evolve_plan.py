@@ -38,8 +38,7 @@ def test_plain_matches_oracle(native, sl, m):
     for q in range(3):
         want = orc.ham_sim(A, P[q], 0.05 * 4, 4, m, substeps=1 << sl)
         assert maxrel(got[q], want) < 1e-12, q
-    k, _ = E.config()
-    assert E.launches_per_step() == (1 << sl) * m * -(-3 // k)   # states share launches, k per launch
+    assert E.launches_per_step() == (1 << sl) * m   # one launch per term covers every state
 
 
 def test_plain_single_state_equals_reference_rule(native):
@@ -104,14 +103,16 @@ def test_plan_rejects_bad_input(native):
 
 
 @pytest.mark.parametrize("cfg", [(8, 1, 0), (8, 2, 0), (8, 4, 0), (4, 2, 0), (4, 4, 0), (2, 4, 0), (1, 4, 0),
-                                 (1, 1, 0), (8, 4, 1), (4, 4, 1), (2, 4, 1), (1, 4, 1)])
+                                 (1, 1, 0), (8, 4, 1), (4, 4, 1), (2, 4, 1), (1, 4, 1),
+                                 (8, 4, 2), (4, 4, 2), (2, 4, 2), (1, 4, 2), (8, 4, 3), (4, 4, 3), (8, 4, 4),
+                                 (2, 4, 4)])
 def test_mixed_every_launch_shape(native, cfg):
     """Each (states per launch, rows per thread, pipelined) shape the autotuner may pick gives
     the same answer (3 states: the last launch of a chunked shape runs with masked slots)."""
     capi, _ = native
     A, E, P, pr, pi = _setup(capi, 11, 3, capi.EVOLVE_MIXED)
     E.set_config(*cfg)
-    assert E.config() == cfg[:2] and E.pipelined() == bool(cfg[2])
+    assert E.config() == cfg[:2] and E.pipelined() == cfg[2]
     E.run(pr, pi, A.rows, 0.05, 5, 0, 13)
     got = _result(pr, pi)
     for q in range(3):
@@ -128,6 +129,21 @@ def test_plain_every_launch_shape(native, cfg):
     got = _result(pr, pi)
     for q in (0, 4):
         assert maxrel(got[q], orc.ham_sim(A, P[q], 0.15, 3, 9, substeps=2)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [3, 7, 16])
+@pytest.mark.parametrize("variant", [2, 3, 4])
+def test_prefetch_kernel_edges(native, n, variant):
+    """The L2-prefetch kernel: 8-row matrices (every strip partial), 7 qubits (one warp strip of
+    128 rows, offsets +-1, +-2 with shuffled windows), 16 qubits (many blocks, all offsets)."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, n, 3, capi.EVOLVE_MIXED)
+    E.set_config(4, 4, variant)
+    E.run(pr, pi, A.rows, 0.05, 3, 0, 11)
+    got = _result(pr, pi)
+    for q in range(3):
+        want = orc.ham_sim(A, P[q], 0.15, 3, 11)
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
 
 
 def test_autotuner_caches_its_choice(native, tmp_path, monkeypatch):

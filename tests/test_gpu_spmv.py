@@ -25,7 +25,8 @@ def _spmv_capi(capi, A: orc.OMatrix, x: np.ndarray, precision=0, nrhs=1, shift=0
     import torch
 
     M = capi.Matrix.create(A.rows, A.cols, A.off, A.re, A.im, precision=precision)
-    dt = torch.float64 if precision == 0 else torch.float32
+    f64 = precision != 1   # c128 and c128f2 take float64 vectors, c64 float32
+    dt = torch.float64 if f64 else torch.float32
     X = np.atleast_2d(x)
     k = X.shape[0]
     xr = torch.zeros(k * A.cols + shift, dtype=dt, device="cuda")
@@ -40,7 +41,7 @@ def _spmv_capi(capi, A: orc.OMatrix, x: np.ndarray, precision=0, nrhs=1, shift=0
     px, pxi = xr.data_ptr() + shift * esz, xi.data_ptr() + shift * esz
     py, pyi = yr.data_ptr() + shift * esz, yi.data_ptr() + shift * esz
     if nrhs == 1 and k == 1:
-        fn = L.diaq_spmv_z if precision == 0 else L.diaq_spmv_c
+        fn = L.diaq_spmv_z if f64 else L.diaq_spmv_c
         capi.check(fn(M.h, px, pxi, py, pyi, s))
     else:
         capi.check(L.diaq_spmm(M.h, k, px, pxi, A.cols, py, pyi, A.rows, s))
