@@ -32,6 +32,9 @@ sys.path.insert(0, ROOT)
 DT = 0.05
 TOL_STEP = 1e-8     # per time step: 100 steps stay within 1e-6 of the exact evolution
 METRIC = "expm(-iHt)·ψ states·steps/s"
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the chosen form's term kernel,
+# from ncu captures (profiles/), keyed by (qubits, states, states per block, rows per thread, variant)
+TRAFFIC_PER_LAUNCH = {(20, 8, 2, 4, 0): 809.8e6}
 
 
 def peaks():
@@ -580,13 +583,21 @@ def run_ours(args, rank, world):
     del Hf, y64r, y64i
 
     peak, peak_kind = peaks()
-    # algorithmic bytes of one chosen time step: per launch the c64 matrix once, per state
-    # v in (8N) + v out (8N) + sum pair read/write (16N each; the first term only writes, the
-    # last reads the pair and read-modify-writes psi in float64 instead of writing the pair)
-    chunks = (S + 7) // 8
-    per_state_step = (1 << s_c) * (m_c * 16 * N + (m_c - 1) * 16 * N + (m_c - 1) * 16 * N + 32 * N - 16 * N)
-    step_bytes = (1 << s_c) * m_c * chunks * 8 * total + S * per_state_step
+    # algorithmic bytes of one chosen time step.  Every Taylor term is one launch over all S
+    # states and reads the c64 matrix once (8 B per stored value).  Per state and term: term in
+    # (8N) and term out (8N); the first term writes the (hi, lo) sum pair (16N), the middle ones
+    # read and write it (32N), the last reads it and read-modify-writes psi in float64 (16N +
+    # 32N) -- 32N + 48N (m - 2) + 64N = 48N m per sub-step.
+    per_state_step = (1 << s_c) * 48 * N * m_c
+    step_bytes = (1 << s_c) * m_c * 8 * total + S * per_state_step
     achieved = step_bytes / (ms / K * 1e-3) / 1e9
+    k_launch, v_launch = chosen.config()
+    variant = chosen.pipelined()
+    kernel = (f"dia_spmv_kernel<float,{k_launch},{v_launch},EpiMixed>" if variant == 0 else
+              f"variant {variant}, {k_launch} states x {v_launch} rows per thread")
+    # DRAM bytes of one launch from the ncu capture of this workload and shape
+    # (profiles/dia_spmv_mixed_k2v4_and_f2_xxz20.md); null for shapes not captured
+    traffic = TRAFFIC_PER_LAUNCH.get((args.n, S, k_launch, v_launch, variant))
     value = world * S * K / (ms / 1e3)
     plain_value = world * K / (ms_plain / 1e3)
     line = {
@@ -596,7 +607,7 @@ def run_ours(args, rank, world):
         "config": {"workload": f"xxz{args.n}_periodic_evolve", "form": "chosen", "n_qubits": args.n, "rows": N,
                    "ndiag": len(off), "stored_values": total, "dt": DT, "states_per_gpu": S,
                    "substeps": 1 << s_c, "taylor_terms": m_c, "selection": selection,
-                   "launch_shape": {"states_per_launch": chosen.config()[0], "rows_per_thread": chosen.config()[1],
+                   "launch_shape": {"states_per_block": chosen.config()[0], "rows_per_thread": chosen.config()[1],
                                     "kernel_variant": chosen.pipelined()},
                    "tol_per_step": TOL_STEP, "norm1": norm1.value,
                    "l2": "inputs larger than L2 (c64 matrix 327 MB, states 128 MB > 129 MB)",
@@ -606,8 +617,10 @@ def run_ours(args, rank, world):
         "plain": {"value": plain_value, "ms_per_step": ms_plain / K, "substeps": 1 << s_p, "taylor_terms": m_p,
                   "launches_per_step": lps_plain, "speedup_chosen_over_plain": value / plain_value},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "dia_spmv_kernel<float,8,EpiMixed>",
-                     "bytes_per_step": step_bytes, "launches_per_step": lps, "peak_kind": peak_kind},
+                     "traffic": traffic, "kernel": kernel, "bytes_per_launch": step_bytes / lps,
+                     "bytes_per_step": step_bytes, "launches_per_step": lps, "peak_kind": peak_kind,
+                     "note": "achieved = algorithmic bytes per launch / mean launch time (CUDA events over the "
+                             "timed steps; every launch of a step is this kernel)"},
         "spmv_c128": {"us": spmv_us, "gbs": (16 * total + 32 * N) / spmv_us / 1e3,
                       "frac": (16 * total + 32 * N) / spmv_us / 1e3 / peak,
                       "dfma_per_launch": 4 * total, "reps": args.spmv_reps},

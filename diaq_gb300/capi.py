@@ -38,6 +38,8 @@ SIGNATURES = {
     "diaq_spmv_host": (INT, [P, P, P, P, P]),
     "diaq_spmv_ntimes_host": (INT, [P, P, P, INT, P, P]),
     "diaq_spmm_dia_device": (INT, [P, P, INT, I64, I64, P, I64, P, INT, P]),
+    "diaq_matrix_from_dense": (INT, [I64, I64, P, INT, INT, P, P]),
+    "diaq_matrix_to_dense": (INT, [P, P, INT, P]),
     "diaq_spgemm_symbolic": (INT, [P, P, P, P, P]),
     "diaq_spgemm_numeric": (INT, [P, P, P, P]),
     "diaq_spgemm": (INT, [P, P, INT, P, P]),
@@ -185,6 +187,25 @@ class Matrix:
         check(fn(self.h, *args, ctypes.byref(out)))
         return Matrix(out)
 
+    @staticmethod
+    def from_dense(a, precision=C128, stream=None) -> "Matrix":
+        """From a dense complex array: a numpy array (copied to the device) or a CUDA torch tensor."""
+        out = ctypes.c_void_p()
+        if hasattr(a, "data_ptr"):
+            rows, cols = a.shape
+            check(lib().diaq_matrix_from_dense(rows, cols, a.data_ptr(), 1, precision, stream, ctypes.byref(out)))
+        else:
+            a = np.ascontiguousarray(a, dtype=np.complex128)
+            rows, cols = a.shape
+            check(lib().diaq_matrix_from_dense(rows, cols, a.ctypes.data, 0, precision, stream, ctypes.byref(out)))
+        return Matrix(out)
+
+    def to_dense(self) -> np.ndarray:
+        rows, cols = self.info()[:2]
+        a = np.empty((rows, cols), dtype=np.complex128)
+        check(lib().diaq_matrix_to_dense(self.h, a.ctypes.data, 0, None))
+        return a
+
     def copy(self):
         return self._new(lib().diaq_matrix_copy, None)
 
@@ -211,14 +232,14 @@ class Evolve:
         """In place on host float64 arrays of nrhs*N values."""
         check(lib().diaq_evolve_run_host(self.h, psi_re.ctypes.data, psi_im.ctypes.data, dt, steps, substeps_log2, m))
 
-    def set_config(self, states_per_launch: int, rows_per_thread: int = 0, pipelined: int = 0):
+    def set_config(self, states_per_block: int, rows_per_thread: int = 0, pipelined: int = 0):
         """Force a launch shape (0 states: automatic, autotuned on the next run).  pipelined: 0
         registers only, 1 cp.async pipeline, 2 / 3 / 4 shuffled state windows with an L2 prefetch of
         the matrix 4 / 8 / 0 diagonals ahead."""
-        check(lib().diaq_evolve_set_config(self.h, states_per_launch, rows_per_thread, int(pipelined)))
+        check(lib().diaq_evolve_set_config(self.h, states_per_block, rows_per_thread, int(pipelined)))
 
     def config(self):
-        """(states per launch, rows per thread) of the current shape."""
+        """(states per block, rows per thread) of the current shape."""
         k, v, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(lib().diaq_evolve_config(self.h, ctypes.byref(k), ctypes.byref(v), ctypes.byref(p)))
         return k.value, v.value

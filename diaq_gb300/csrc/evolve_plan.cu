@@ -345,7 +345,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
             if (P.cfg.pipe >= 2) {
                 DQ_TRY(launch_dia_spmv_pf<EpiMixed>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg.kmax, P.cfg.pipe,
                                                     &P.launches_per_step));
-            } else if (P.cfg.pipe) {
+            } else if (P.cfg.pipe == 1) {
                 DQ_TRY(launch_dia_spmv_pipe<EpiMixed>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg.kmax,
                                                       &P.launches_per_step));
             } else {
@@ -375,7 +375,7 @@ static std::string cache_path() {
     return std::string(home ? home : "/tmp") + "/.cache/diaq_gb300/autotune.json";
 }
 
-// The cache is a flat JSON object {"key": [states_per_launch, rows_per_thread, pipelined], ...}.
+// The cache is a flat JSON object {"key": [states_per_block, rows_per_thread, pipelined], ...}.
 static std::map<std::string, SpmvCfg> read_cache() {
     std::map<std::string, SpmvCfg> out;
     std::ifstream f(cache_path());
@@ -580,22 +580,22 @@ int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld,
 
 int diaq_evolve_launches_per_step(diaq_evolve_t E) { return E ? E->launches_per_step : 0; }
 
-int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread, int pipelined) {
+int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_thread, int pipelined) {
     if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
-    if (states_per_launch == 0) {  // back to automatic choice
+    if (states_per_block == 0) {  // back to automatic choice
         E->tuned = false;
         E->cfg = SpmvCfg{};
     } else {
         const bool f32 = E->mode == DIAQ_EVOLVE_MIXED;
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
-        if (states_per_launch < 1 || states_per_launch > 8 || !vr_ok)
-            return set_error(DIAQ_ERR_INVALID, "evolve: states_per_launch in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
+        if (states_per_block < 1 || states_per_block > 8 || !vr_ok)
+            return set_error(DIAQ_ERR_INVALID, "evolve: states_per_block in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
         if (pipelined < 0 || pipelined > 4)
             return set_error(DIAQ_ERR_INVALID,
                              "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), 4 (shuffled windows)");
         if (pipelined && !(f32 && rows_per_thread == 4))
             return set_error(DIAQ_ERR_INVALID, "evolve: the pipelined kernels are the mixed mode's, with 4 rows per thread");
-        E->cfg = SpmvCfg{states_per_launch, rows_per_thread, pipelined};
+        E->cfg = SpmvCfg{states_per_block, rows_per_thread, pipelined};
         E->tuned = true;
     }
     for (auto &kv : E->graphs) cudaGraphExecDestroy(kv.second);
@@ -613,9 +613,9 @@ int diaq_evolve_set_renormalize(diaq_evolve_t E, int on) {
     return DIAQ_OK;
 }
 
-int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread, int *pipelined) {
-    if (!E || !states_per_launch || !rows_per_thread) return set_error(DIAQ_ERR_INVALID, "NULL argument");
-    *states_per_launch = E->cfg.kmax;
+int diaq_evolve_config(diaq_evolve_t E, int *states_per_block, int *rows_per_thread, int *pipelined) {
+    if (!E || !states_per_block || !rows_per_thread) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    *states_per_block = E->cfg.kmax;
     *rows_per_thread = E->cfg.vr > 0 ? E->cfg.vr : (E->mode == DIAQ_EVOLVE_MIXED ? 4 : 2);
     if (pipelined) *pipelined = E->cfg.pipe;
     return DIAQ_OK;

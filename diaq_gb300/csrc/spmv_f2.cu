@@ -19,6 +19,7 @@
 // Storage: the layout of the other precisions, the re (im) array holding the hi plane of
 // `capacity` floats followed by the lo plane.
 #include <algorithm>
+#include <cstdlib>
 
 #include "spmv_kernel.cuh"
 
@@ -103,8 +104,8 @@ __device__ __forceinline__ void f2_prefetch_strip(const DiagMeta &m, int64_t w0,
     prefetch_l2_bulk(aim + cap + m.base + a, bytes);
 }
 
-template <int PF>
-__global__ void __launch_bounds__(kSpmvThreads)
+template <int PF, int MINB>
+__global__ void __launch_bounds__(kSpmvThreads, MINB)
     f2_spmv_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                    const float *__restrict__ aim, int64_t cap, int64_t rows, const float *__restrict__ xrh,
                    const float *__restrict__ xrl, const float *__restrict__ xih, const float *__restrict__ xil,
@@ -248,7 +249,12 @@ int f2_spmv(const Matrix &A, const double *xr, const double *xi, double *yr, dou
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * num_sms()));
     f2_split_vec_kernel<<<g, 256, 0, s>>>(xr, xrh, xrl, n);
     f2_split_vec_kernel<<<g, 256, 0, s>>>(xi, xih, xil, n);
-    f2_spmv_kernel<0><<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
+    static const int minb = [] {
+        const char *v = std::getenv("DIAQ_F2_MINB");
+        return v ? std::atoi(v) : 3;
+    }();
+    auto kern = minb >= 6 ? f2_spmv_kernel<0, 6> : minb == 5 ? f2_spmv_kernel<0, 5> : f2_spmv_kernel<0, 4>;
+    kern<<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
                                                                   (const float *)A.im, A.capacity, A.rows, xrh, xrl,
                                                                   xih, xil, yr, yi);
     cudaError_t e = cudaGetLastError();

@@ -412,13 +412,13 @@ inline unsigned spmv_blocks(int64_t rows, int V) {
 struct SpmvCfg {
     int kmax = 8;
     int vr = 0;
-    int pipe = 0;  // float kernels, 4 rows per thread: 1 cp.async pipeline; shuffled windows with L2 prefetch
-                   // 4 (2) or 8 (3) diagonals ahead, or without prefetch (4)
+    int pipe = 0;  // kernel variant: 0 registers; float kernels with 4 rows per thread: 1 cp.async pipeline,
+                   // shuffled windows with L2 prefetch 4 (2) or 8 (3) diagonals ahead or none (4)
 };
 
 template <typename T, int K, class Epi, int VR, int... More>
-void launch_vr(int vr, const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, int nchunk, const Epi &e,
-               cudaStream_t s) {
+void launch_vr(int vr, const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, int nchunk,
+               const Epi &e, cudaStream_t s) {
     if constexpr (sizeof...(More) > 0) {
         if (vr != VR) {
             launch_vr<T, K, Epi, More...>(vr, A, xr, xi, ldx, nrhs, nchunk, e, s);

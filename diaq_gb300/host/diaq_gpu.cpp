@@ -359,6 +359,26 @@ PYBIND11_MODULE(diaq_gpu, m) {
         return from_dense(a.data(), shape[0], shape[1]);
     });
     m.def("to_numpy", &to_dense);
+    m.def("to_numpy", [](const DevPtr &A) {  // dense array written on the GPU, then copied once
+        int64_t r, c, t;
+        int32_t nd;
+        int p;
+        A->info(r, c, nd, t, p);
+        py::array_t<cplx> out({r, c});
+        check(diaq_matrix_to_dense(A->h, reinterpret_cast<double *>(out.mutable_data()), 0, nullptr));
+        return out;
+    });
+    m.def(
+        "from_numpy_device",
+        [](py::array_t<cplx, py::array::c_style | py::array::forcecast> a, const std::string &precision) {
+            if (a.ndim() != 2) throw std::runtime_error("from_numpy: expected a 2-D array");
+            diaq_matrix_t h = nullptr;
+            check(diaq_matrix_from_dense(a.shape(0), a.shape(1), reinterpret_cast<const double *>(a.data()), 0,
+                                         parse_precision(precision), nullptr, &h));
+            return std::make_shared<DeviceMatrix>(h);
+        },
+        py::arg("arr"), py::arg("precision") = "c128",
+        "from_numpy straight to a DeviceMatrix: the nonzero diagonals are found and gathered on the GPU.");
     m.def("from_numpy_vector", &vec_from_numpy);
     m.def("to_numpy_vector", &vec_to_numpy);
     m.def(

@@ -112,6 +112,19 @@ int diaq_matrix_from_pauli(int n_qubits, int32_t n_strings, const double *coeff_
                            const double *coeff_im, const uint64_t *x_mask, const uint64_t *z_mask,
                            int precision, void *stream, diaq_matrix_t *out);
 
+/* A device matrix from a dense rows x cols array of interleaved complex128 values, row-major
+ * (numpy / torch complex128), on the device (on_device != 0) or the host: the diagonals holding
+ * a value other than exact zero, in ascending order, as from_numpy builds them
+ * (src/dense_to_diagonals.hpp:20-58, include/pythonWrappers.cpp:146-193), but on the GPU.
+ * Synchronous. */
+int diaq_matrix_from_dense(int64_t rows, int64_t cols, const double *dense, int on_device,
+                           int precision, void *stream, diaq_matrix_t *out);
+
+/* The dense rows x cols array (interleaved complex128, row-major) of A, written on the device
+ * (on_device != 0; asynchronous on stream) or the host (synchronous).  Replaces to_numpy(A)
+ * after DeviceMatrix.to_host() (include/pythonWrappers.cpp:195-218, src/deviceMatrix_gpu.cu:62-113). */
+int diaq_matrix_to_dense(diaq_matrix_t A, double *dense, int on_device, void *stream);
+
 /* ------------------------------------------------------------------------------------------
  * SpMV.  Replaces spmv_device (src/spMV_gpu.cu:142-168): y = A x on device arrays, y
  * overwritten, asynchronous on stream.
@@ -232,8 +245,10 @@ int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld,
 int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
                          int substeps_log2, int m);
 
-/* Launch shape of the plan's term kernel: states per launch (1..8; the matrix is read once per
- * launch), rows per thread (1, 2, or 4 for the mixed mode) and, for the mixed mode with 4 rows,
+/* Launch shape of the plan's term kernel: states per block (1..8: one launch covers every state,
+ * in chunks of this many per block, the chunks of a row tile side by side so that the matrix
+ * tile comes from HBM about once), rows per thread (1, 2, or 4 for the mixed mode) and, for the
+ * mixed mode with 4 rows,
  * the kernel variant `pipelined`: 0 registers only, 1 stream the next diagonals through shared
  * memory with asynchronous copies, 2 / 3 / 4 read unaligned state windows as aligned vectors
  * shifted across lanes and prefetch the matrix into L2 4 / 8 / 0 diagonals ahead.
@@ -241,8 +256,8 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
  * two steps of scratch copies of the states and keeps the fastest, caching the choice in a JSON
  * file (DIAQ_AUTOTUNE_CACHE, else $HOME/.cache/diaq_gb300/autotune.json).  Setting a shape drops
  * the recorded graphs.  pipelined may be NULL in diaq_evolve_config. */
-int diaq_evolve_set_config(diaq_evolve_t E, int states_per_launch, int rows_per_thread, int pipelined);
-int diaq_evolve_config(diaq_evolve_t E, int *states_per_launch, int *rows_per_thread, int *pipelined);
+int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_thread, int pipelined);
+int diaq_evolve_config(diaq_evolve_t E, int *states_per_block, int *rows_per_thread, int *pipelined);
 
 /* on != 0: after every step rescale each state to norm 1, the norm computed in float64 (the
  * exact evolution is unitary; this removes the drift of the truncated series).  Off by default:

@@ -120,7 +120,7 @@ def test_mixed_every_launch_shape(native, cfg):
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
 
 
-@pytest.mark.parametrize("cfg", [(8, 1), (8, 2), (4, 2), (2, 2), (1, 2), (1, 1)])
+@pytest.mark.parametrize("cfg", [(8, 1, 0), (8, 2, 0), (4, 2, 0), (2, 2, 0), (1, 2, 0), (1, 1, 0)])
 def test_plain_every_launch_shape(native, cfg):
     capi, _ = native
     A, E, P, pr, pi = _setup(capi, 10, 5, capi.EVOLVE_C128)
