@@ -223,13 +223,37 @@ def _max_over_ranks(ms, world, dev):
     return ms
 
 
-def _barrier(world):
+def _sum_over_ranks(v, world, dev):
     import torch
 
-    torch.cuda.synchronize()
+    if world > 1:
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        v = float(t.item())
+    return v
+
+
+def _barrier(world, cuda=True):
+    import torch
+
+    if cuda:
+        torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
+    if cuda:
+        torch.cuda.synchronize()
+
+
+def partition_instances(costs, world):
+    """Independent instances to ranks: largest first, each to the least-loaded rank (ties to the
+    lower rank), so every rank gets about the same work; returns one index list per rank."""
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in sorted(range(len(costs)), key=lambda j: (-costs[j], j)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(i)
+        load[r] += costs[i]
+    return [sorted(p) for p in parts]
 
 
 def run_spmv_only(args):
@@ -350,6 +374,13 @@ def run_batched(args):
     from diaq_gb300 import hamiltonians as ham
     from oracle import oracle as orc
 
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dev = "cuda"
+    if world > 1:  # replicas: every rank evolves its share of the instances, no data exchange
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+        dev = torch.device("cuda", torch.cuda.current_device())
     build.build()
     L = capi.lib()
     rng = np.random.default_rng(args.batch_seed)
@@ -359,9 +390,12 @@ def run_batched(args):
         model = "tfim" if i % 2 == 0 else "xxz"
         k = int(rng.choice([1, 4, 16]))
         specs.append((model, n, k, _pauli_chain(model, n, rng)))
+    all_states = int(sum(k for _, _, k, _ in specs))
+    mine = partition_instances([k * (2 * n + 1) * (1 << n) for _, n, k, _ in specs], world)[rank]
+    specs = [specs[i] for i in mine]
     dt, tol = 0.02, TOL_STEP
-    out = {"mode": "batched", "instances": len(specs), "n_range": [args.n_lo, args.n_hi], "dt": dt,
-           "states": int(sum(k for _, _, k, _ in specs)), "variants": {}}
+    out = {"mode": "batched", "instances": args.instances, "n_range": [args.n_lo, args.n_hi], "dt": dt,
+           "states": all_states, "n_gpus": world, "scaling": "weak" if world > 1 else None, "variants": {}}
     for variant in (["c64", "c128"] if args.variant == "both" else [args.variant]):
         prec = capi.C64 if variant == "c64" else capi.C128
         w = 8 if variant == "c64" else 16
@@ -418,13 +452,18 @@ def run_batched(args):
             cfg = B.config()
             del B, mats, prs, pis
             torch.cuda.empty_cache()
+        total_ms = _max_over_ranks(total_ms, world, dev)
+        total_states_steps = _sum_over_ranks(total_states_steps, world, dev)
         out["variants"][variant] = {"value": total_states_steps / (total_ms / 1e3), "unit": "states·steps/s",
                                     "steps": steps, "groups": len(groups), "ms": total_ms,
                                     "launch_shape": {"states_per_launch": cfg[0], "rows_per_thread": cfg[1],
                                                      "phases_per_step_last_group": cfg[2]},
                                     "rel_err_vs_oracle_max": max(checks) if checks else None,
                                     "checked_instances": len(checks)}
-    print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 def run_precision(args):

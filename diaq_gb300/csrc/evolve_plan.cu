@@ -171,7 +171,7 @@ __global__ void norm_partial_kernel(const double *__restrict__ pr, const double 
 }
 
 __global__ void renorm_kernel(double *__restrict__ pr, double *__restrict__ pi, float *__restrict__ fr,
-                              float *__restrict__ fi, int64_t n, const double *__restrict__ part) {
+                              float *__restrict__ fi, int64_t n, const double *__restrict__ part, int sp) {
     const int q = blockIdx.y;
     __shared__ double inv;
     if (threadIdx.x == 0) {
@@ -186,9 +186,10 @@ __global__ void renorm_kernel(double *__restrict__ pr, double *__restrict__ pi, 
         const double x = a[i] * c, y = b[i] * c;
         a[i] = x;
         b[i] = y;
-        if (fr) {
-            fr[(int64_t)q * n + i] = (float)x;
-            fi[(int64_t)q * n + i] = (float)y;
+        if (fr) {  // the float32 copy: planar (sp = 0) or interleaved
+            const int64_t j = sp ? i * sp + q : (int64_t)q * n + i;
+            fr[j] = (float)x;
+            fi[j] = (float)y;
         }
     }
 }
@@ -196,6 +197,129 @@ __global__ void renorm_kernel(double *__restrict__ pr, double *__restrict__ pi, 
 __global__ void to_f32_kernel(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         b[i] = (float)a[i];
+}
+
+// ---- interleaved states (kernel variant 6) ----------------------------------------------------------
+// The float32 work vectors of the mixed mode hold the states interleaved per row: element (r, q)
+// at v[r * sp + q], sp = nrhs rounded up to a multiple of 4 (the padding states are zero).  A
+// state window at any diagonal offset is then sp contiguous floats per row, 16-byte aligned, so
+// every thread reads four states of one row with one vector load per array, whatever the offset
+// (the planar layout splits the windows of offsets that are not multiples of 4).  Thread t owns
+// row t / (sp/4) and states 4 (t mod sp/4) .. +3; the threads of a row share the matrix value
+// (an L1 broadcast).  Few registers per thread: 8 blocks of 256 threads fit on an SM.
+
+// psi (state q at p[q * ld + r]) -> interleaved float32, padding states zero.
+__global__ void to_f32_il_kernel(const double *__restrict__ pr, const double *__restrict__ pi, int64_t ld,
+                                 int64_t n, int nrhs, int sp, float *__restrict__ fr, float *__restrict__ fi) {
+    const int64_t cnt = n * sp;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / sp;
+        const int q = (int)(e - r * sp);
+        fr[e] = q < nrhs ? (float)pr[q * ld + r] : 0.f;
+        fi[e] = q < nrhs ? (float)pi[q * ld + r] : 0.f;
+    }
+}
+
+// One Taylor term's epilogue for four interleaved states of one row; the arithmetic of EpiMixed.
+struct EpiMixedIL {
+    float *vr, *vi;                 // term out (interleaved)
+    float *hr, *hi_, *lr, *li;      // compensated sum (interleaved)
+    double *pr, *pi;                // state, q at p[q * ld + r]
+    int64_t ld;
+    int sp, nrhs;
+    float scale;
+    int first, last;
+    __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
+        const int64_t i = r * sp + 4 * g;
+        float tr[4], ti[4], h_r[4], h_i[4], l_r[4], l_i[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tr[c] = si[c] * scale;
+            ti[c] = -sr[c] * scale;
+        }
+        if (first) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                h_r[c] = tr[c];
+                h_i[c] = ti[c];
+                l_r[c] = l_i[c] = 0.f;
+            }
+        } else {
+            const float4 a = *reinterpret_cast<const float4 *>(hr + i), b = *reinterpret_cast<const float4 *>(hi_ + i);
+            const float4 c4 = *reinterpret_cast<const float4 *>(lr + i), d = *reinterpret_cast<const float4 *>(li + i);
+            const float ha[4] = {a.x, a.y, a.z, a.w}, hb[4] = {b.x, b.y, b.z, b.w};
+            const float la[4] = {c4.x, c4.y, c4.z, c4.w}, lb[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float e_r, e_i;
+                two_sum(ha[c], tr[c], h_r[c], e_r);
+                two_sum(hb[c], ti[c], h_i[c], e_i);
+                l_r[c] = la[c] + e_r;
+                l_i[c] = lb[c] + e_i;
+            }
+        }
+        if (!last) {
+            *reinterpret_cast<float4 *>(hr + i) = make_float4(h_r[0], h_r[1], h_r[2], h_r[3]);
+            *reinterpret_cast<float4 *>(hi_ + i) = make_float4(h_i[0], h_i[1], h_i[2], h_i[3]);
+            *reinterpret_cast<float4 *>(lr + i) = make_float4(l_r[0], l_r[1], l_r[2], l_r[3]);
+            *reinterpret_cast<float4 *>(li + i) = make_float4(l_i[0], l_i[1], l_i[2], l_i[3]);
+            *reinterpret_cast<float4 *>(vr + i) = make_float4(tr[0], tr[1], tr[2], tr[3]);
+            *reinterpret_cast<float4 *>(vi + i) = make_float4(ti[0], ti[1], ti[2], ti[3]);
+        } else {
+            float nr_[4], ni_[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int q = 4 * g + c;
+                nr_[c] = ni_[c] = 0.f;
+                if (q < nrhs) {
+                    const double nr = pr[q * ld + r] + ((double)h_r[c] + (double)l_r[c]);
+                    const double ni = pi[q * ld + r] + ((double)h_i[c] + (double)l_i[c]);
+                    pr[q * ld + r] = nr;
+                    pi[q * ld + r] = ni;
+                    nr_[c] = (float)nr;
+                    ni_[c] = (float)ni;
+                }
+            }
+            *reinterpret_cast<float4 *>(vr + i) = make_float4(nr_[0], nr_[1], nr_[2], nr_[3]);
+            *reinterpret_cast<float4 *>(vi + i) = make_float4(ni_[0], ni_[1], ni_[2], ni_[3]);
+        }
+    }
+};
+
+__global__ void __launch_bounds__(kSpmvThreads)
+    dia_spmv_il_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
+                       const float *__restrict__ aim, int64_t rows, const float *__restrict__ xr,
+                       const float *__restrict__ xi, EpiMixedIL epi) {
+    __shared__ DiagMeta sm[kMetaChunk];
+    const int sp = epi.sp, quads = sp >> 2;
+    const int64_t t = (int64_t)blockIdx.x * kSpmvThreads + threadIdx.x;
+    const int64_t r = t / quads;
+    const int g = (int)(t - r * quads);
+    float accr[4] = {0.f, 0.f, 0.f, 0.f}, acci[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
+        const int cn = min(kMetaChunk, nd - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
+        __syncthreads();
+        if (r >= rows) continue;
+#pragma unroll 4
+        for (int k = 0; k < cn; ++k) {
+            if (r < sm[k].lo || r >= sm[k].hi) continue;
+            const float a = __ldcs(are + sm[k].base + r), b = __ldcs(aim + sm[k].base + r);
+            const int64_t c = (r + sm[k].off) * sp + 4 * g;
+            const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + c));
+            const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + c));
+            const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                accr[q] = fmaf(a, xv[q], accr[q]);
+                accr[q] = fmaf(-b, yv[q], accr[q]);
+                acci[q] = fmaf(a, yv[q], acci[q]);
+                acci[q] = fmaf(b, xv[q], acci[q]);
+            }
+        }
+    }
+    if (r < rows) epi.apply(r, g, accr, acci);
 }
 
 // ---- the plan ------------------------------------------------------------------------------------------
@@ -221,6 +345,11 @@ struct EvolvePlan {
     bool tuned = false;   // cfg chosen (by the autotuner or the caller)
     bool renorm = false;  // rescale every state to norm 1 (float64) after each step
     double *part = nullptr;  // renormalisation partial sums, nrhs * kNormBlocks
+    int sp = 4;           // nrhs rounded up to a multiple of 4 (interleaved layout)
+
+    bool interleaved() const { return mode == DIAQ_EVOLVE_MIXED && cfg.pipe == 6; }
+    // floats per float32 work vector (all states)
+    int64_t vlen() const { return (interleaved() ? (int64_t)sp : (int64_t)nrhs) * n; }
 
     ~EvolvePlan() {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -248,10 +377,13 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     P->mode = mode;
     P->nrhs = nrhs;
     P->n = H.rows;
+    P->sp = (nrhs + 3) / 4 * 4;
     int st = DIAQ_OK;
     cudaError_t e = cudaStreamCreateWithFlags(&P->s, cudaStreamNonBlocking);
     const size_t vec = (size_t)nrhs * (size_t)P->n;
-    const size_t bytes = mode == DIAQ_EVOLVE_C128 ? 6 * vec * sizeof(double) : 8 * vec * sizeof(float);
+    // the mixed mode sizes its 8 float vectors for the interleaved layout (>= nrhs states)
+    const size_t bytes = mode == DIAQ_EVOLVE_C128 ? 6 * vec * sizeof(double)
+                                                  : 8 * (size_t)P->sp * (size_t)P->n * sizeof(float);
     if (e == cudaSuccess && bytes) e = cudaMalloc(&P->buf, bytes);
     if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
     if (st == DIAQ_OK && mode == DIAQ_EVOLVE_MIXED) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
@@ -263,12 +395,19 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     return DIAQ_OK;
 }
 
+// The partial sums of the renormalisation; allocated before any step is recorded (no
+// allocation is allowed while a stream is being captured).
+static int ensure_renorm_buffer(EvolvePlan &P) {
+    if (P.renorm && !P.part) DQ_CUDA(cudaMalloc(&P.part, sizeof(double) * kNormBlocks * P.nrhs));
+    return DIAQ_OK;
+}
+
 static int enqueue_renorm(EvolvePlan &P, double *pr, double *pi, float *fr, float *fi) {
     if (!P.renorm) return DIAQ_OK;
-    if (!P.part) DQ_CUDA(cudaMalloc(&P.part, sizeof(double) * kNormBlocks * P.nrhs));
+    if (!P.part) return set_error(DIAQ_ERR_INVALID, "evolve: renormalisation buffer missing");
     const dim3 g(kNormBlocks, (unsigned)P.nrhs);
     norm_partial_kernel<<<g, 256, 0, P.s>>>(pr, pi, P.n, P.part);
-    renorm_kernel<<<g, 256, 0, P.s>>>(pr, pi, fr, fi, P.n, P.part);
+    renorm_kernel<<<g, 256, 0, P.s>>>(pr, pi, fr, fi, P.n, P.part, P.interleaved() ? P.sp : 0);
     DQ_CUDA(cudaGetLastError());
     P.launches_per_step += 2;
     return DIAQ_OK;
@@ -322,13 +461,25 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
     }
     // MIXED
     float *w = (float *)P.buf;
-    const int64_t L = n;
+    const int64_t L = n, VL = P.vlen();
     if (ld != n) return set_error(DIAQ_ERR_UNSUPPORTED, "evolve mixed: psi leading dimension must equal N");
-    float *var = w, *vai = w + k * L, *vbr = w + 2 * k * L, *vbi = w + 3 * k * L;
-    float *hr = w + 4 * k * L, *hi = w + 5 * k * L, *lr = w + 6 * k * L, *li = w + 7 * k * L;
+    float *var = w, *vai = w + VL, *vbr = w + 2 * VL, *vbi = w + 3 * VL;
+    float *hr = w + 4 * VL, *hi = w + 5 * VL, *lr = w + 6 * VL, *li = w + 7 * VL;
     float *in_r = var, *in_i = vai, *out_r = vbr, *out_i = vbi;  // v_a holds fp32(psi) on entry
     for (int j = 0; j < sub; ++j) {
         for (int t = 1; t <= m; ++t) {
+            if (P.interleaved()) {
+                EpiMixedIL e{out_r, out_i, hr, hi, lr, li, pr, pi, ld, P.sp, (int)k, (float)(tau / (double)t),
+                             t == 1, t == m};
+                const int64_t threads = n * (P.sp / 4);
+                dia_spmv_il_kernel<<<(unsigned)((threads + kSpmvThreads - 1) / kSpmvThreads), kSpmvThreads, 0, P.s>>>(
+                    P.Hc->d_meta, P.Hc->nd, (const float *)P.Hc->re, (const float *)P.Hc->im, n, in_r, in_i, e);
+                DQ_CUDA(cudaGetLastError());
+                ++P.launches_per_step;
+                std::swap(in_r, out_r);
+                std::swap(in_i, out_i);
+                continue;
+            }
             EpiMixed e;
             e.vr = out_r;
             e.vi = out_i;
@@ -357,10 +508,27 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
         }
     }
     if (in_r != var) {  // an odd number of launches: put fp32(psi) back where the next step reads it
-        DQ_CUDA(cudaMemcpyAsync(var, in_r, sizeof(float) * k * L, cudaMemcpyDeviceToDevice, P.s));
-        DQ_CUDA(cudaMemcpyAsync(vai, in_i, sizeof(float) * k * L, cudaMemcpyDeviceToDevice, P.s));
+        DQ_CUDA(cudaMemcpyAsync(var, in_r, sizeof(float) * VL, cudaMemcpyDeviceToDevice, P.s));
+        DQ_CUDA(cudaMemcpyAsync(vai, in_i, sizeof(float) * VL, cudaMemcpyDeviceToDevice, P.s));
     }
     return enqueue_renorm(P, pr, pi, var, vai);
+}
+
+// fp32(psi) into v_a, in the layout of the plan's current kernel (psi with leading dimension n).
+static int fp32_state(EvolvePlan &P, const double *pr, const double *pi, cudaStream_t s) {
+    float *var = (float *)P.buf, *vai = var + P.vlen();
+    if (P.interleaved()) {
+        const int64_t cnt = P.n * P.sp;
+        const int grid = (int)std::min<int64_t>((cnt + 255) / 256, 8 * num_sms());
+        to_f32_il_kernel<<<grid, 256, 0, s>>>(pr, pi, P.n, P.n, P.nrhs, P.sp, var, vai);
+    } else {
+        const int64_t cnt = P.nrhs * P.n;
+        const int grid = (int)std::min<int64_t>((cnt + 255) / 256, 8 * num_sms());
+        to_f32_kernel<<<grid, 256, 0, s>>>(pr, var, cnt);
+        to_f32_kernel<<<grid, 256, 0, s>>>(pi, vai, cnt);
+    }
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
 }
 
 // ---- autotuner ----------------------------------------------------------------------------------------
@@ -439,7 +607,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
                 {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
                 {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
-                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}};
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}};
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -479,10 +647,8 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     for (size_t c = 0; c < cand.size() && st == DIAQ_OK; ++c) {
         P.cfg = cand[c];
         if (P.mode == DIAQ_EVOLVE_MIXED) {
-            float *var = (float *)P.buf, *vai = var + cnt;
-            const int grid = (int)std::min<int64_t>(((int64_t)cnt + 255) / 256, 8 * num_sms());
-            to_f32_kernel<<<grid, 256, 0, P.s>>>(tmp, var, (int64_t)cnt);
-            to_f32_kernel<<<grid, 256, 0, P.s>>>(tmp + cnt, vai, (int64_t)cnt);
+            st = fp32_state(P, tmp, tmp + cnt, P.s);
+            if (st != DIAQ_OK) break;
         }
         st = enqueue_step(P, dt, sl, m, tmp, tmp + cnt, P.n);  // warm-up
         if (st != DIAQ_OK) break;
@@ -519,6 +685,7 @@ static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt
     if (steps < 0 || m < 0 || sl < 0 || sl > 20) return set_error(DIAQ_ERR_INVALID, "evolve: bad steps / s / m");
     if (!pr || !pi) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
     if (steps == 0 || m == 0 || P.n == 0) return DIAQ_OK;
+    DQ_TRY(ensure_renorm_buffer(P));
     if (!P.tuned) DQ_TRY(autotune(P, dt, sl, m, pr, pi, ld, user));
     const EvolvePlan::Key key{dt, sl, m, pr, pi, ld};
     auto it = P.graphs.find(key);
@@ -541,14 +708,7 @@ static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt
         it = P.graphs.emplace(key, ge).first;
     }
     // everything below runs on the caller's stream
-    if (P.mode == DIAQ_EVOLVE_MIXED) {  // fp32(psi) into v_a for the first sub-step
-        float *var = (float *)P.buf, *vai = var + P.nrhs * P.n;
-        const int64_t cnt = P.nrhs * P.n;
-        const int grid = (int)std::min<int64_t>((cnt + 255) / 256, 8 * num_sms());
-        to_f32_kernel<<<grid, 256, 0, user>>>(pr, var, cnt);
-        to_f32_kernel<<<grid, 256, 0, user>>>(pi, vai, cnt);
-        DQ_CUDA(cudaGetLastError());
-    }
+    if (P.mode == DIAQ_EVOLVE_MIXED) DQ_TRY(fp32_state(P, pr, pi, user));  // fp32(psi) for the first sub-step
     for (int64_t i = 0; i < steps; ++i) DQ_CUDA(cudaGraphLaunch(it->second, user));
     return DIAQ_OK;
 }
@@ -590,11 +750,16 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_block < 1 || states_per_block > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_block in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
-        if (pipelined < 0 || pipelined > 4)
-            return set_error(DIAQ_ERR_INVALID,
-                             "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), 4 (shuffled windows)");
-        if (pipelined && !(f32 && rows_per_thread == 4))
+        if (pipelined < 0 || pipelined > 6 || pipelined == 5)
+            return set_error(DIAQ_ERR_INVALID, "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), "
+                                               "4 (shuffled windows), 6 (interleaved states)");
+        if (pipelined == 6) {
+            if (!(f32 && states_per_block == 4 && rows_per_thread == 1))
+                return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernel is the mixed mode's, 4 states and "
+                                                   "1 row per thread");
+        } else if (pipelined && !(f32 && rows_per_thread == 4)) {
             return set_error(DIAQ_ERR_INVALID, "evolve: the pipelined kernels are the mixed mode's, with 4 rows per thread");
+        }
         E->cfg = SpmvCfg{states_per_block, rows_per_thread, pipelined};
         E->tuned = true;
     }

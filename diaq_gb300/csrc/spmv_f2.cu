@@ -19,7 +19,6 @@
 // Storage: the layout of the other precisions, the re (im) array holding the hi plane of
 // `capacity` floats followed by the lo plane.
 #include <algorithm>
-#include <cstdlib>
 
 #include "spmv_kernel.cuh"
 
@@ -249,12 +248,9 @@ int f2_spmv(const Matrix &A, const double *xr, const double *xi, double *yr, dou
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * num_sms()));
     f2_split_vec_kernel<<<g, 256, 0, s>>>(xr, xrh, xrl, n);
     f2_split_vec_kernel<<<g, 256, 0, s>>>(xi, xih, xil, n);
-    static const int minb = [] {
-        const char *v = std::getenv("DIAQ_F2_MINB");
-        return v ? std::atoi(v) : 3;
-    }();
-    auto kern = minb >= 6 ? f2_spmv_kernel<0, 6> : minb == 5 ? f2_spmv_kernel<0, 5> : f2_spmv_kernel<0, 4>;
-    kern<<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
+    // four blocks per SM (64 registers): 166.8 us on the 20-qubit chain; three (80 registers)
+    // 189 us, five or six spill (252, 339 us)
+    f2_spmv_kernel<0, 4><<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
                                                                   (const float *)A.im, A.capacity, A.rows, xrh, xrl,
                                                                   xih, xil, yr, yi);
     cudaError_t e = cudaGetLastError();

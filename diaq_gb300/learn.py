@@ -88,6 +88,30 @@ def chain(H: capi.Matrix, psi, M: int = M_CHAIN):
     return U
 
 
+def chain_stats(H: capi.Matrix, psi, M: int = M_CHAIN):
+    """The norms ||u_k||, k = 0..M, of the chain of `chain` and |<u_0, u_1>|, without storing the
+    chain: what the features and the a-posteriori check need at selection time."""
+    import torch
+
+    L = capi.lib()
+    xr = psi.real.contiguous()
+    xi = psi.imag.contiguous()
+    x0r, x0i = xr.clone(), xi.clone()
+    yr, yi = torch.empty_like(xr), torch.empty_like(xi)
+    s = torch.cuda.current_stream().cuda_stream
+    norms = [torch.sqrt(torch.dot(xr, xr) + torch.dot(xi, xi))]
+    v01 = None
+    for k in range(1, M + 1):
+        capi.check(L.diaq_spmv_z(H.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), s))
+        xr = yi / k
+        xi = -yr / k
+        norms.append(torch.sqrt(torch.dot(xr, xr) + torch.dot(xi, xi)))
+        if k == 1:   # <u_0, u_1> = conj(u_0) . u_1
+            v01 = torch.complex(torch.dot(x0r, xr) + torch.dot(x0i, xi), torch.dot(x0r, xi) - torch.dot(x0i, xr))
+    unorm = torch.stack(norms).cpu().numpy()
+    return unorm, float(torch.abs(v01).item())
+
+
 def tails(U, tau: float, m_max: int = M_MAX):
     """||sum_{k>m} tau^k u_k|| for m = 1..m_max (float64 numpy), and ||tau^k u_k|| for k = 0..M."""
     import torch
@@ -109,12 +133,11 @@ def norm_bound(norm1: float, t: float, tol: float):
     return capi.select_sm(norm1, t, tol, 1.0, 100)
 
 
-def features(n, H: capi.Matrix, U, t, tol, norm1, fro):
+def features(n, H: capi.Matrix, unorm, v01, t, tol, norm1, fro):
+    """16 features from the matrix, the chain norms unorm = ||u_k|| and v01 = |<u_0, u_1>|."""
     N, _, nd, _, _ = H.info()
     off = H.offsets()
-    import torch
-
-    un = torch.linalg.vector_norm(U[:5], dim=1).cpu().numpy()
+    un = unorm[:5]
     s_ref, m_ref = norm_bound(norm1, t, tol)
     theta = t * norm1
     f = np.zeros(16, dtype=np.float32)
@@ -130,7 +153,7 @@ def features(n, H: capi.Matrix, U, t, tol, norm1, fro):
         f[6 + k] = math.log10(max(t * hk ** (1.0 / k), 1e-30))
     f[11] = math.log10(max(fro / math.sqrt(N), 1e-30))
     # u_1 = -i H psi, so <psi, H psi> = i <u_0, u_1>
-    f[12] = float(torch.abs(torch.vdot(U[0], U[1])).item()) / max(un[1], 1e-300)
+    f[12] = v01 / max(un[1], 1e-300)
     f[13] = s_ref / 20
     f[14] = min(m_ref, 100) / 30
     f[15] = math.log10(max(2 * un[2] / max(un[1] ** 2, 1e-300), 1e-30))
@@ -157,15 +180,15 @@ def label(U, t, tol, norm1):
     return best
 
 
-def check(U, t, tol, norm1, s, m):
-    """The a-posteriori next-term test of a proposal (see the module docstring)."""
+def check(unorm, t, tol, norm1, s, m):
+    """The a-posteriori next-term test of a proposal (see the module docstring); unorm[k] = ||u_k||."""
     if not (0 <= s <= S_MAX and 1 <= m <= M_MAX):
         return False
     tau = t / 2 ** s
     if tau * norm1 / (m + 2) > 0.5:
         return False
-    _, term = tails(U, tau)
-    return 2 ** s * 2 * term[m + 1] <= tol
+    term = math.exp((m + 1) * math.log(tau)) * float(unorm[m + 1]) if tau > 0 else 0.0
+    return 2 ** s * 2 * term <= tol
 
 
 def instance_record(n, terms, t, tol, seed):
@@ -183,10 +206,18 @@ def record_for(H: capi.Matrix, n, t, tol, seed, with_label=True):
     capi.check(capi.lib().diaq_frobenius(H.h, ctypes.byref(fro), None))
     N = 1 << n
     psi = torch.from_numpy(ham.random_state(N, seed)).cuda()
-    U = chain(H, psi)
-    f = features(n, H, U, t, tol, norm1.value, fro.value)
-    lab = label(U, t, tol, norm1.value) if with_label else None
-    return {"f": f, "label": lab, "norm1": norm1.value, "U": U, "H": H, "ref": norm_bound(norm1.value, t, tol)}
+    rec = {"norm1": norm1.value, "H": H, "ref": norm_bound(norm1.value, t, tol), "label": None}
+    if with_label:   # the whole chain: labels need the exact tails
+        U = chain(H, psi)
+        unorm = torch.linalg.vector_norm(U, dim=1).cpu().numpy()
+        v01 = float(torch.abs(torch.vdot(U[0], U[1])).item())
+        rec["U"] = U
+        rec["label"] = label(U, t, tol, norm1.value)
+    else:            # selection only: norms, streamed
+        unorm, v01 = chain_stats(H, psi)
+    rec["unorm"] = unorm
+    rec["f"] = features(n, H, unorm, v01, t, tol, norm1.value, fro.value)
+    return rec
 
 
 def generate(count, seed, n_lo=8, n_hi=16, log_every=1000):
@@ -270,7 +301,7 @@ def choose(net, record, t, tol):
     for mm in range(max(1, m - 3), min(M_MAX, m + 4) + 1):
         if 2 ** s * mm > 2 ** s_ref * m_ref:
             break
-        if check(record["U"], t, tol, record["norm1"], s, mm):
+        if check(record["unorm"], t, tol, record["norm1"], s, mm):
             return s, mm, "learned"
     return s_ref, m_ref, "norm-bound"
 

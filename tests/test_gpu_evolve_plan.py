@@ -105,7 +105,7 @@ def test_plan_rejects_bad_input(native):
 @pytest.mark.parametrize("cfg", [(8, 1, 0), (8, 2, 0), (8, 4, 0), (4, 2, 0), (4, 4, 0), (2, 4, 0), (1, 4, 0),
                                  (1, 1, 0), (8, 4, 1), (4, 4, 1), (2, 4, 1), (1, 4, 1),
                                  (8, 4, 2), (4, 4, 2), (2, 4, 2), (1, 4, 2), (8, 4, 3), (4, 4, 3), (8, 4, 4),
-                                 (2, 4, 4)])
+                                 (2, 4, 4), (4, 1, 6)])
 def test_mixed_every_launch_shape(native, cfg):
     """Each (states per launch, rows per thread, pipelined) shape the autotuner may pick gives
     the same answer (3 states: the last launch of a chunked shape runs with masked slots)."""
@@ -144,6 +144,27 @@ def test_prefetch_kernel_edges(native, n, variant):
     for q in range(3):
         want = orc.ham_sim(A, P[q], 0.15, 3, 11)
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
+
+
+@pytest.mark.parametrize("k,sl,m,renorm", [(5, 0, 11, False), (5, 1, 7, True), (8, 0, 12, False), (3, 2, 5, True)])
+def test_interleaved_states(native, k, sl, m, renorm):
+    """Kernel variant 6 (states interleaved per row, padded to a multiple of 4): odd and even
+    launch counts, sub-steps, renormalisation, padding states."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 11, k, capi.EVOLVE_MIXED)
+    E.set_config(4, 1, 6)
+    E.set_renormalize(renorm)
+    E.run(pr, pi, A.rows, 0.05, 4, sl, m)
+    got = _result(pr, pi)
+    for q in range(k):
+        want = orc.ham_sim(A, P[q], 0.2, 4, m, substeps=1 << sl)
+        if renorm:
+            want = orc.ham_sim(A, P[q], 0.05, 1, m, substeps=1 << sl)
+            for _ in range(3):
+                want = want / np.linalg.norm(want)
+                want = orc.ham_sim(A, want, 0.05, 1, m, substeps=1 << sl)
+            want = want / np.linalg.norm(want)
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, q
 
 
 def test_autotuner_caches_its_choice(native, tmp_path, monkeypatch):

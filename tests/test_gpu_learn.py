@@ -60,3 +60,22 @@ def test_trained_selector_gains_over_norm_bound(native):
             assert r["err"] <= r["tol"]
     gain = np.mean([r["cost_ref"] / r["cost"] for r in rows])
     assert gain > 1.0, gain
+
+
+def test_selection_streams_the_chain(native):
+    """At selection time the chain is not stored: its norms and <u0, u1> are streamed, and the
+    features and the checked choice equal those computed from the stored chain."""
+    from diaq_gb300 import learn
+
+    rng = np.random.default_rng(21)
+    for _ in range(4):
+        n, terms, t, tol = learn.random_instance(rng, 9, 11)
+        H = learn.build(n, terms)
+        full = learn.record_for(H, n, t, tol, seed=77, with_label=True)
+        lean = learn.record_for(H, n, t, tol, seed=77, with_label=False)
+        assert "U" not in lean
+        assert np.allclose(lean["unorm"], full["unorm"], rtol=1e-12, atol=0)
+        assert np.allclose(lean["f"], full["f"], rtol=1e-6, atol=1e-7)
+        net = learn.load()
+        if net is not None:
+            assert learn.choose(net, lean, t, tol) == learn.choose(net, full, t, tol)
