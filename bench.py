@@ -33,8 +33,9 @@ DT = 0.05
 TOL_STEP = 1e-8     # per time step: 100 steps stay within 1e-6 of the exact evolution
 METRIC = "expm(-iHt)·ψ states·steps/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the chosen form's term kernel,
-# from ncu captures (profiles/), keyed by (qubits, states, states per block, rows per thread, variant)
-TRAFFIC_PER_LAUNCH = {(20, 8, 2, 4, 0): 809.8e6}
+# from ncu captures (profiles/), keyed by (qubits, states, form, states per block, rows per thread,
+# variant)
+TRAFFIC_PER_LAUNCH = {(20, 8, "mixed", 2, 4, 0): 809.8e6}
 
 
 def peaks():
@@ -330,7 +331,7 @@ def run_chosen_only(args):
     norm1 = ctypes.c_double()
     capi.check(L.diaq_norm1_est(H.h, ctypes.byref(norm1), None))
     s_c, m_c, _ = chosen_schedule(capi, H, norm1.value)
-    E = capi.Evolve(H, args.states, capi.EVOLVE_MIXED)
+    E = capi.Evolve(H, args.states, capi.EVOLVE_HORNER if args.horner else capi.EVOLVE_MIXED)
     if args.shape:
         k, v, p = (int(x) for x in args.shape.split(","))
         E.set_config(k, v, p)
@@ -340,7 +341,7 @@ def run_chosen_only(args):
     sp = torch.cuda.current_stream().cuda_stream
     E.run(pr, pi, N, DT, args.warmup, s_c, m_c, sp)
     ms = _timed(torch.cuda.current_stream(), lambda: E.run(pr, pi, N, DT, args.steps, s_c, m_c, sp))
-    print(json.dumps({"mode": "chosen", "n_qubits": args.n, "states": args.states, "s": s_c, "m": m_c,
+    print(json.dumps({"mode": "chosen", "horner": args.horner, "n_qubits": args.n, "states": args.states, "s": s_c, "m": m_c,
                       "shape": list(E.config()) + [E.pipelined()],
                       "ms_per_step": ms / args.steps, "us_per_launch": 1e3 * ms / args.steps / E.launches_per_step()}),
           flush=True)
@@ -550,9 +551,11 @@ def run_ours(args, rank, world):
     ms_plain = _max_over_ranks(_timed(stream, lambda: plain.run(ppr, ppi, N, DT, K, s_p, m_p, sp)), world, dev)
     lps_plain = plain.launches_per_step()
 
-    # ---- chosen form: S states per launch, complex64 terms + FP64 state, learned (s, m) ----
+    # ---- chosen form: all S states per launch, complex64 matrix, float32 Horner evaluation,
+    # FP64 state, learned (s, m) ----
+    CHOSEN_MODE = capi.EVOLVE_HORNER
     s_c, m_c, selection = chosen_schedule(capi, H, norm1.value)
-    chosen = capi.Evolve(H, S, capi.EVOLVE_MIXED)
+    chosen = capi.Evolve(H, S, CHOSEN_MODE)
     P0 = ham.random_state(N, 0, k=S) if S > 1 else p0[None, :]
     cpr = torch.from_numpy(np.ascontiguousarray(P0.real)).to(dev)
     cpi = torch.from_numpy(np.ascontiguousarray(P0.imag)).to(dev)
@@ -580,7 +583,7 @@ def run_ours(args, rank, world):
     # ---- end to end through the C ABI with host buffers: S states up, K steps, S states down ----
     hr = np.ascontiguousarray(P0.real).ravel().copy()
     hi = np.ascontiguousarray(P0.imag).ravel().copy()
-    e2e_plan = capi.Evolve(H, S, capi.EVOLVE_MIXED)
+    e2e_plan = capi.Evolve(H, S, CHOSEN_MODE)
     e2e_plan.run_host(hr.copy(), hi.copy(), DT, 1, s_c, m_c)   # graph recorded outside the timed region
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -623,27 +626,29 @@ def run_ours(args, rank, world):
 
     peak, peak_kind = peaks()
     # algorithmic bytes of one chosen time step.  Every Taylor term is one launch over all S
-    # states and reads the c64 matrix once (8 B per stored value).  Per state and term: term in
-    # (8N) and term out (8N); the first term writes the (hi, lo) sum pair (16N), the middle ones
-    # read and write it (32N), the last reads it and read-modify-writes psi in float64 (16N +
-    # 32N) -- 32N + 48N (m - 2) + 64N = 48N m per sub-step.
-    per_state_step = (1 << s_c) * 48 * N * m_c
+    # states and reads the c64 matrix once (8 B per stored value).  Per state, Horner form: the
+    # first term reads fp32(psi) (8N; its window and its epilogue read the same vector) and writes
+    # w (8N); a middle term reads w and fp32(psi) and writes the next w (24N); the last reads w,
+    # read-modify-writes psi in float64 and writes fp32(psi) (8N + 32N + 8N) -- (24 m + 16) N per
+    # sub-step for m >= 2.
+    per_state_step = (1 << s_c) * (24 * m_c + 16) * N
     step_bytes = (1 << s_c) * m_c * 8 * total + S * per_state_step
     achieved = step_bytes / (ms / K * 1e-3) / 1e9
     k_launch, v_launch = chosen.config()
     variant = chosen.pipelined()
-    kernel = (f"dia_spmv_kernel<float,{k_launch},{v_launch},EpiMixed>" if variant == 0 else
+    kernel = (f"dia_spmv_il_kernel<EpiHornerIL,{[0, 4, 8][variant - 6]}>" if variant >= 6 else
+              f"dia_spmv_kernel<float,{k_launch},{v_launch},EpiHorner>" if variant == 0 else
               f"variant {variant}, {k_launch} states x {v_launch} rows per thread")
-    # DRAM bytes of one launch from the ncu capture of this workload and shape
-    # (profiles/dia_spmv_mixed_k2v4_and_f2_xxz20.md); null for shapes not captured
-    traffic = TRAFFIC_PER_LAUNCH.get((args.n, S, k_launch, v_launch, variant))
+    # DRAM bytes of one launch from the ncu capture of this workload, form and shape (profiles/);
+    # null for shapes not captured
+    traffic = TRAFFIC_PER_LAUNCH.get((args.n, S, "horner", k_launch, v_launch, variant))
     value = world * S * K / (ms / 1e3)
     plain_value = world * K / (ms_plain / 1e3)
     line = {
         "metric": METRIC, "value": value, "unit": "states·steps/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 terms + f64 state", "data": "synthetic (seeded XXZ couplings and states, built in-process)",
-        "config": {"workload": f"xxz{args.n}_periodic_evolve", "form": "chosen", "n_qubits": args.n, "rows": N,
+        "config": {"workload": f"xxz{args.n}_periodic_evolve", "form": "chosen", "evaluation": "horner", "n_qubits": args.n, "rows": N,
                    "ndiag": len(off), "stored_values": total, "dt": DT, "states_per_gpu": S,
                    "substeps": 1 << s_c, "taylor_terms": m_c, "selection": selection,
                    "launch_shape": {"states_per_block": chosen.config()[0], "rows_per_thread": chosen.config()[1],
@@ -689,6 +694,7 @@ def main():
     ap.add_argument("--spmv-reps", type=int, default=1000)
     ap.add_argument("--states", type=int, default=8, help="states evolved together by the chosen form")
     ap.add_argument("--shape", default="", help="chosen mode: force the launch shape 'states,rows,pipelined'")
+    ap.add_argument("--horner", action="store_true", help="chosen mode: Horner-form evaluation (DIAQ_EVOLVE_HORNER)")
     ap.add_argument("--instances", type=int, default=512, help="batched mode: Hamiltonians")
     ap.add_argument("--n-lo", type=int, default=10)
     ap.add_argument("--n-hi", type=int, default=22)

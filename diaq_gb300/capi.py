@@ -16,7 +16,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libdiaq_gb300.so")
 
 C128, C64, C128F2 = 0, 1, 2
-EVOLVE_C128, EVOLVE_MIXED = 0, 1
+EVOLVE_C128, EVOLVE_MIXED, EVOLVE_HORNER = 0, 1, 2
 _lib = None
 
 # name -> (restype, argtypes); mirrors include/diaq_gb300.h

@@ -7,6 +7,10 @@
 //
 // Modes
 //  DIAQ_EVOLVE_C128   plain: complex128 matrix, vectors and sums (the reference's arithmetic).
+//  DIAQ_EVOLVE_HORNER complex64 matrix; p(A) psi = psi + A (psi + A/2 (psi + ... A/m psi)),
+//                     A = -i tau H, evaluated from the inside out in float32: each term reads
+//                     the previous w and fp32(psi) and writes the next w; the outermost step
+//                     adds A w_1 to psi in float64 and refreshes fp32(psi).
 //  DIAQ_EVOLVE_MIXED  complex64 matrix and Taylor terms, the running sum of one sub-step kept as a
 //                     compensated (hi, lo) pair of floats (TwoSum per term), and the state itself
 //                     in float64: psi <- psi + (hi + lo) in double at the end of every sub-step.
@@ -142,6 +146,54 @@ struct EpiMixed {
                     pi[i] = ni;
                     vr[i] = (float)nr;
                     vi[i] = (float)ni;
+                }
+            }
+    }
+};
+
+// One Horner step: w_out = fp32(psi) + (-i * scale) (A w_in); on the outermost step (last)
+// psi += (-i * scale) (A w_1) in float64 and the fresh fp32(psi) goes to g (which is not the
+// fp32(psi) this launch reads when the step's SpMV also reads it, m = 1).
+struct EpiHorner {
+    float *wr, *wi;                 // w out
+    const float *fr, *fi;           // fp32(psi)
+    double *pr, *pi;                // psi
+    float *gr, *gi;                 // fp32(psi) written on the last step
+    int64_t ld;
+    float scale;
+    int last;
+    __host__ __device__ EpiHorner shifted(int q0) const {
+        EpiHorner e = *this;
+        const int64_t o = q0 * ld;
+        e.wr += o;
+        e.wi += o;
+        e.fr += o;
+        e.fi += o;
+        e.pr += o;
+        e.pi += o;
+        e.gr += o;
+        e.gi += o;
+        return e;
+    }
+    template <typename U, int K, int V>
+    __device__ __forceinline__ void apply(int64_t r0, int64_t rows, int kq, U (&sr)[K][V], U (&si)[K][V]) const {
+#pragma unroll
+        for (int q = 0; q < K; ++q)
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int64_t r = r0 + v;
+                if (q >= kq || r >= rows) continue;
+                const int64_t i = q * ld + r;
+                const float tr = si[q][v] * scale, ti = -sr[q][v] * scale;
+                if (!last) {
+                    wr[i] = fr[i] + tr;
+                    wi[i] = fi[i] + ti;
+                } else {
+                    const double nr = pr[i] + (double)tr, ni = pi[i] + (double)ti;
+                    pr[i] = nr;
+                    pi[i] = ni;
+                    gr[i] = (float)nr;
+                    gi[i] = (float)ni;
                 }
             }
     }
@@ -286,36 +338,109 @@ struct EpiMixedIL {
     }
 };
 
+// The Horner step (EpiHorner) for four interleaved states of one row.
+struct EpiHornerIL {
+    float *wr, *wi;                 // interleaved: w out
+    const float *fr, *fi;           // fp32(psi)
+    float *gr, *gi;                 // fp32(psi) written on the last step
+    double *pr, *pi;                // psi, q at p[q * ld + r]
+    int64_t ld;
+    int sp, nrhs;
+    float scale;
+    int last;
+    __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
+        const int64_t i = r * sp + 4 * g;
+        float tr[4], ti[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tr[c] = si[c] * scale;
+            ti[c] = -sr[c] * scale;
+        }
+        if (!last) {
+            const float4 a = *reinterpret_cast<const float4 *>(fr + i), b = *reinterpret_cast<const float4 *>(fi + i);
+            *reinterpret_cast<float4 *>(wr + i) = make_float4(a.x + tr[0], a.y + tr[1], a.z + tr[2], a.w + tr[3]);
+            *reinterpret_cast<float4 *>(wi + i) = make_float4(b.x + ti[0], b.y + ti[1], b.z + ti[2], b.w + ti[3]);
+        } else {
+            float nr_[4], ni_[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int q = 4 * g + c;
+                nr_[c] = ni_[c] = 0.f;
+                if (q < nrhs) {
+                    const double nr = pr[q * ld + r] + (double)tr[c], ni = pi[q * ld + r] + (double)ti[c];
+                    pr[q * ld + r] = nr;
+                    pi[q * ld + r] = ni;
+                    nr_[c] = (float)nr;
+                    ni_[c] = (float)ni;
+                }
+            }
+            *reinterpret_cast<float4 *>(gr + i) = make_float4(nr_[0], nr_[1], nr_[2], nr_[3]);
+            *reinterpret_cast<float4 *>(gi + i) = make_float4(ni_[0], ni_[1], ni_[2], ni_[3]);
+        }
+    }
+};
+
+// D > 0: the matrix values (one float per plane and row) of the next D diagonals are loaded
+// into a register ring ahead of use, so a thread has D HBM reads of the matrix stream in flight
+// and waits on each diagonal only for its state windows (L2 hits, mostly).
+template <class Epi, int D>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_il_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                        const float *__restrict__ aim, int64_t rows, const float *__restrict__ xr,
-                       const float *__restrict__ xi, EpiMixedIL epi) {
+                       const float *__restrict__ xi, Epi epi) {
     __shared__ DiagMeta sm[kMetaChunk];
     const int sp = epi.sp, quads = sp >> 2;
     const int64_t t = (int64_t)blockIdx.x * kSpmvThreads + threadIdx.x;
     const int64_t r = t / quads;
     const int g = (int)(t - r * quads);
     float accr[4] = {0.f, 0.f, 0.f, 0.f}, acci[4] = {0.f, 0.f, 0.f, 0.f};
+    auto term = [&](const DiagMeta &m, float a, float b) {
+        const int64_t c = (r + m.off) * sp + 4 * g;
+        const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + c));
+        const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + c));
+        const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            accr[q] = fmaf(a, xv[q], accr[q]);
+            accr[q] = fmaf(-b, yv[q], accr[q]);
+            acci[q] = fmaf(a, yv[q], acci[q]);
+            acci[q] = fmaf(b, xv[q], acci[q]);
+        }
+    };
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, nd - c0);
         __syncthreads();
         for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
         __syncthreads();
         if (r >= rows) continue;
+        if constexpr (D == 0) {
 #pragma unroll 4
-        for (int k = 0; k < cn; ++k) {
-            if (r < sm[k].lo || r >= sm[k].hi) continue;
-            const float a = __ldcs(are + sm[k].base + r), b = __ldcs(aim + sm[k].base + r);
-            const int64_t c = (r + sm[k].off) * sp + 4 * g;
-            const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + c));
-            const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + c));
-            const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
+            for (int k = 0; k < cn; ++k) {
+                if (r < sm[k].lo || r >= sm[k].hi) continue;
+                term(sm[k], __ldcs(are + sm[k].base + r), __ldcs(aim + sm[k].base + r));
+            }
+        } else {
+            // ring slot d holds diagonal k0 + d; rows outside a diagonal load nothing (value 0)
+            float ra[D], rb[D];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                accr[q] = fmaf(a, xv[q], accr[q]);
-                accr[q] = fmaf(-b, yv[q], accr[q]);
-                acci[q] = fmaf(a, yv[q], acci[q]);
-                acci[q] = fmaf(b, xv[q], acci[q]);
+            for (int d = 0; d < D; ++d) {
+                const bool in = d < cn && r >= sm[d].lo && r < sm[d].hi;
+                ra[d] = in ? __ldcs(are + sm[d].base + r) : 0.f;
+                rb[d] = in ? __ldcs(aim + sm[d].base + r) : 0.f;
+            }
+            for (int k0 = 0; k0 < cn; k0 += D) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    const int k = k0 + d;
+                    if (k < cn) {
+                        const float a = ra[d], b = rb[d];
+                        const int kn = k + D;
+                        const bool in = kn < cn && r >= sm[kn].lo && r < sm[kn].hi;
+                        ra[d] = in ? __ldcs(are + sm[kn].base + r) : 0.f;
+                        rb[d] = in ? __ldcs(aim + sm[kn].base + r) : 0.f;
+                        if (r >= sm[k].lo && r < sm[k].hi) term(sm[k], a, b);
+                    }
+                }
             }
         }
     }
@@ -347,7 +472,8 @@ struct EvolvePlan {
     double *part = nullptr;  // renormalisation partial sums, nrhs * kNormBlocks
     int sp = 4;           // nrhs rounded up to a multiple of 4 (interleaved layout)
 
-    bool interleaved() const { return mode == DIAQ_EVOLVE_MIXED && cfg.pipe == 6; }
+    bool f32() const { return mode == DIAQ_EVOLVE_MIXED || mode == DIAQ_EVOLVE_HORNER; }
+    bool interleaved() const { return f32() && cfg.pipe >= 6; }
     // floats per float32 work vector (all states)
     int64_t vlen() const { return (interleaved() ? (int64_t)sp : (int64_t)nrhs) * n; }
 
@@ -367,11 +493,28 @@ struct diaq_evolve_s : public diaq_gb300::EvolvePlan {};
 
 namespace diaq_gb300 {
 
+// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4) or 8 (ring of 8).
+template <class Epi>
+int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &e) {
+    const int64_t threads = P.n * (P.sp / 4);
+    const unsigned g = (unsigned)((threads + kSpmvThreads - 1) / kSpmvThreads);
+    const float *are = (const float *)P.Hc->re, *aim = (const float *)P.Hc->im;
+    if (P.cfg.pipe == 7)
+        dia_spmv_il_kernel<Epi, 4><<<g, kSpmvThreads, 0, P.s>>>(P.Hc->d_meta, P.Hc->nd, are, aim, P.n, xr, xi, e);
+    else if (P.cfg.pipe == 8)
+        dia_spmv_il_kernel<Epi, 8><<<g, kSpmvThreads, 0, P.s>>>(P.Hc->d_meta, P.Hc->nd, are, aim, P.n, xr, xi, e);
+    else
+        dia_spmv_il_kernel<Epi, 0><<<g, kSpmvThreads, 0, P.s>>>(P.Hc->d_meta, P.Hc->nd, are, aim, P.n, xr, xi, e);
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
+}
+
 static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     if (H.rows != H.cols) return set_error(DIAQ_ERR_INVALID, "evolve: H must be square");
     if (H.prec != DIAQ_C128) return set_error(DIAQ_ERR_INVALID, "evolve: pass the c128 matrix (the plan makes its own c64 copy)");
     if (nrhs < 1) return set_error(DIAQ_ERR_INVALID, "evolve: nrhs must be >= 1");
-    if (mode != DIAQ_EVOLVE_C128 && mode != DIAQ_EVOLVE_MIXED) return set_error(DIAQ_ERR_INVALID, "evolve: unknown mode");
+    if (mode != DIAQ_EVOLVE_C128 && mode != DIAQ_EVOLVE_MIXED && mode != DIAQ_EVOLVE_HORNER)
+        return set_error(DIAQ_ERR_INVALID, "evolve: unknown mode");
     EvolvePlan *P = new diaq_evolve_s();
     P->H = &H;
     P->mode = mode;
@@ -386,7 +529,7 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
                                                   : 8 * (size_t)P->sp * (size_t)P->n * sizeof(float);
     if (e == cudaSuccess && bytes) e = cudaMalloc(&P->buf, bytes);
     if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
-    if (st == DIAQ_OK && mode == DIAQ_EVOLVE_MIXED) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
+    if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
     if (st != DIAQ_OK) {
         delete static_cast<diaq_evolve_s *>(P);
         return st;
@@ -459,6 +602,41 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
         }
         return enqueue_renorm(P, pr, pi, nullptr, nullptr);
     }
+    if (P.mode == DIAQ_EVOLVE_HORNER) {
+        float *w = (float *)P.buf;
+        const int64_t L = n, VL = P.vlen();
+        if (ld != n) return set_error(DIAQ_ERR_UNSUPPORTED, "evolve horner: psi leading dimension must equal N");
+        float *fr = w, *fi = w + VL, *war = w + 2 * VL, *wai = w + 3 * VL, *wbr = w + 4 * VL, *wbi = w + 5 * VL;
+        for (int j = 0; j < sub; ++j) {
+            const float *in_r = fr, *in_i = fi;  // w_m = psi
+            float *out_r = war, *out_i = wai;
+            for (int t = 1; t <= m; ++t) {
+                const float scale = (float)(tau / (double)(m - t + 1));
+                const bool last = (t == m);
+                // the last step refreshes fp32(psi); when it also reads fp32(psi) (m = 1) it writes
+                // the fresh copy to the free w vector, copied back after the launch
+                float *gr = (last && in_r == fr) ? out_r : fr, *gi = (last && in_r == fr) ? out_i : fi;
+                if (P.interleaved()) {
+                    EpiHornerIL e{out_r, out_i, fr, fi, gr, gi, pr, pi, ld, P.sp, (int)k, scale, last};
+                    DQ_TRY(launch_il(P, in_r, in_i, e));
+                } else {
+                    EpiHorner e{out_r, out_i, fr, fi, pr, pi, gr, gi, L, scale, last};
+                    DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiHorner, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s,
+                                                                            P.cfg)));
+                }
+                ++P.launches_per_step;
+                if (gr != fr) {
+                    DQ_CUDA(cudaMemcpyAsync(fr, gr, sizeof(float) * VL, cudaMemcpyDeviceToDevice, P.s));
+                    DQ_CUDA(cudaMemcpyAsync(fi, gi, sizeof(float) * VL, cudaMemcpyDeviceToDevice, P.s));
+                }
+                in_r = out_r;
+                in_i = out_i;
+                out_r = (out_r == war) ? wbr : war;
+                out_i = (out_i == wai) ? wbi : wai;
+            }
+        }
+        return enqueue_renorm(P, pr, pi, fr, fi);
+    }
     // MIXED
     float *w = (float *)P.buf;
     const int64_t L = n, VL = P.vlen();
@@ -471,10 +649,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
             if (P.interleaved()) {
                 EpiMixedIL e{out_r, out_i, hr, hi, lr, li, pr, pi, ld, P.sp, (int)k, (float)(tau / (double)t),
                              t == 1, t == m};
-                const int64_t threads = n * (P.sp / 4);
-                dia_spmv_il_kernel<<<(unsigned)((threads + kSpmvThreads - 1) / kSpmvThreads), kSpmvThreads, 0, P.s>>>(
-                    P.Hc->d_meta, P.Hc->nd, (const float *)P.Hc->re, (const float *)P.Hc->im, n, in_r, in_i, e);
-                DQ_CUDA(cudaGetLastError());
+                DQ_TRY(launch_il(P, in_r, in_i, e));
                 ++P.launches_per_step;
                 std::swap(in_r, out_r);
                 std::swap(in_i, out_i);
@@ -597,17 +772,18 @@ static std::string tune_key(const EvolvePlan &P, int sl, int m) {
         if (ch == '"' || ch == ' ') ch = '_';
     char buf[256];
     std::snprintf(buf, sizeof(buf), "%s|%s|n=%lld|nd=%d|k=%d|s=%d|m=%d", name.c_str(),
-                  P.mode == DIAQ_EVOLVE_MIXED ? "mixed" : "c128", (long long)P.n, P.H->nd, P.nrhs, sl, m);
+                  P.mode == DIAQ_EVOLVE_MIXED ? "mixed" : P.mode == DIAQ_EVOLVE_HORNER ? "horner" : "c128",
+                  (long long)P.n, P.H->nd, P.nrhs, sl, m);
     return buf;
 }
 
 static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double *pi, int64_t ld, cudaStream_t user) {
     std::vector<SpmvCfg> cand;
-    if (P.mode == DIAQ_EVOLVE_MIXED)
+    if (P.f32())
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
                 {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
                 {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
-                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}};
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}};
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -646,7 +822,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     if (e != cudaSuccess) st = cuda_status(e, "autotune", __FILE__, __LINE__);
     for (size_t c = 0; c < cand.size() && st == DIAQ_OK; ++c) {
         P.cfg = cand[c];
-        if (P.mode == DIAQ_EVOLVE_MIXED) {
+        if (P.f32()) {
             st = fp32_state(P, tmp, tmp + cnt, P.s);
             if (st != DIAQ_OK) break;
         }
@@ -708,7 +884,7 @@ static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt
         it = P.graphs.emplace(key, ge).first;
     }
     // everything below runs on the caller's stream
-    if (P.mode == DIAQ_EVOLVE_MIXED) DQ_TRY(fp32_state(P, pr, pi, user));  // fp32(psi) for the first sub-step
+    if (P.f32()) DQ_TRY(fp32_state(P, pr, pi, user));  // fp32(psi) for the first sub-step
     for (int64_t i = 0; i < steps; ++i) DQ_CUDA(cudaGraphLaunch(it->second, user));
     return DIAQ_OK;
 }
@@ -746,14 +922,14 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
         E->tuned = false;
         E->cfg = SpmvCfg{};
     } else {
-        const bool f32 = E->mode == DIAQ_EVOLVE_MIXED;
+        const bool f32 = E->f32();
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_block < 1 || states_per_block > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_block in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
-        if (pipelined < 0 || pipelined > 6 || pipelined == 5)
+        if (pipelined < 0 || pipelined > 8 || pipelined == 5)
             return set_error(DIAQ_ERR_INVALID, "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), "
-                                               "4 (shuffled windows), 6 (interleaved states)");
-        if (pipelined == 6) {
+                                               "4 (shuffled windows), 6, 7, 8 (interleaved states)");
+        if (pipelined >= 6) {
             if (!(f32 && states_per_block == 4 && rows_per_thread == 1))
                 return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernel is the mixed mode's, 4 states and "
                                                    "1 row per thread");
@@ -781,7 +957,7 @@ int diaq_evolve_set_renormalize(diaq_evolve_t E, int on) {
 int diaq_evolve_config(diaq_evolve_t E, int *states_per_block, int *rows_per_thread, int *pipelined) {
     if (!E || !states_per_block || !rows_per_thread) return set_error(DIAQ_ERR_INVALID, "NULL argument");
     *states_per_block = E->cfg.kmax;
-    *rows_per_thread = E->cfg.vr > 0 ? E->cfg.vr : (E->mode == DIAQ_EVOLVE_MIXED ? 4 : 2);
+    *rows_per_thread = E->cfg.vr > 0 ? E->cfg.vr : (E->f32() ? 4 : 2);
     if (pipelined) *pipelined = E->cfg.pipe;
     return DIAQ_OK;
 }

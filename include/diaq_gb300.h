@@ -49,8 +49,12 @@ typedef enum {
 
 typedef enum {
     DIAQ_EVOLVE_C128 = 0, /* complex128 throughout (the reference's arithmetic) */
-    DIAQ_EVOLVE_MIXED = 1 /* complex64 matrix and Taylor terms, compensated float sums,
-                             float64 state */
+    DIAQ_EVOLVE_MIXED = 1, /* complex64 matrix and Taylor terms, compensated float sums,
+                              float64 state */
+    DIAQ_EVOLVE_HORNER = 2 /* complex64 matrix, the Taylor polynomial evaluated in Horner form
+                              in float32 (w_k = psi + A w_{k+1} / (k+1), w_m = psi), the last
+                              step psi + A w_1 in float64: no running sum, half the state
+                              traffic of DIAQ_EVOLVE_MIXED */
 } diaq_evolve_mode;
 
 typedef struct diaq_matrix_s *diaq_matrix_t;
@@ -247,11 +251,13 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
 
 /* Launch shape of the plan's term kernel: states per block (1..8: one launch covers every state,
  * in chunks of this many per block, the chunks of a row tile side by side so that the matrix
- * tile comes from HBM about once), rows per thread (1, 2, or 4 for the mixed mode) and, for the
- * mixed mode with 4 rows,
- * the kernel variant `pipelined`: 0 registers only, 1 stream the next diagonals through shared
- * memory with asynchronous copies, 2 / 3 / 4 read unaligned state windows as aligned vectors
- * shifted across lanes and prefetch the matrix into L2 4 / 8 / 0 diagonals ahead.
+ * tile comes from HBM about once), rows per thread (1, 2, or 4 for the float32 modes) and the
+ * kernel variant `pipelined`: 0 registers only; for the float32 modes with 4 rows, 1 streams the
+ * next diagonals through shared memory with asynchronous copies, 2 / 3 / 4 read unaligned state
+ * windows as aligned vectors shifted across lanes and prefetch the matrix into L2 4 / 8 / 0
+ * diagonals ahead; for the float32 modes with (4 states, 1 row), 6 / 7 / 8 keep the work vectors
+ * interleaved per row (any window one aligned vector) and load the matrix 0 / 4 / 8 diagonals
+ * ahead into registers.
  * 0 states = choose automatically: on the first run the autotuner times the candidate shapes on
  * two steps of scratch copies of the states and keeps the fastest, caching the choice in a JSON
  * file (DIAQ_AUTOTUNE_CACHE, else $HOME/.cache/diaq_gb300/autotune.json).  Setting a shape drops

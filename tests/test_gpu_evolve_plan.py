@@ -105,7 +105,7 @@ def test_plan_rejects_bad_input(native):
 @pytest.mark.parametrize("cfg", [(8, 1, 0), (8, 2, 0), (8, 4, 0), (4, 2, 0), (4, 4, 0), (2, 4, 0), (1, 4, 0),
                                  (1, 1, 0), (8, 4, 1), (4, 4, 1), (2, 4, 1), (1, 4, 1),
                                  (8, 4, 2), (4, 4, 2), (2, 4, 2), (1, 4, 2), (8, 4, 3), (4, 4, 3), (8, 4, 4),
-                                 (2, 4, 4), (4, 1, 6)])
+                                 (2, 4, 4), (4, 1, 6), (4, 1, 7), (4, 1, 8)])
 def test_mixed_every_launch_shape(native, cfg):
     """Each (states per launch, rows per thread, pipelined) shape the autotuner may pick gives
     the same answer (3 states: the last launch of a chunked shape runs with masked slots)."""
@@ -146,13 +146,14 @@ def test_prefetch_kernel_edges(native, n, variant):
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
 
 
+@pytest.mark.parametrize("variant", [6, 7])
 @pytest.mark.parametrize("k,sl,m,renorm", [(5, 0, 11, False), (5, 1, 7, True), (8, 0, 12, False), (3, 2, 5, True)])
-def test_interleaved_states(native, k, sl, m, renorm):
+def test_interleaved_states(native, k, sl, m, renorm, variant):
     """Kernel variant 6 (states interleaved per row, padded to a multiple of 4): odd and even
     launch counts, sub-steps, renormalisation, padding states."""
     capi, _ = native
     A, E, P, pr, pi = _setup(capi, 11, k, capi.EVOLVE_MIXED)
-    E.set_config(4, 1, 6)
+    E.set_config(4, 1, variant)
     E.set_renormalize(renorm)
     E.run(pr, pi, A.rows, 0.05, 4, sl, m)
     got = _result(pr, pi)
@@ -165,6 +166,38 @@ def test_interleaved_states(native, k, sl, m, renorm):
                 want = orc.ham_sim(A, want, 0.05, 1, m, substeps=1 << sl)
             want = want / np.linalg.norm(want)
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, q
+
+
+@pytest.mark.parametrize("cfg", [(8, 4, 0), (2, 4, 0), (4, 2, 0), (8, 1, 0), (4, 1, 6), (4, 1, 8)])
+@pytest.mark.parametrize("sl,m", [(0, 12), (1, 7), (0, 1)])
+def test_horner_accuracy(native, cfg, sl, m):
+    """Horner-form float32 evaluation: within 1e-6 of the FP64 oracle after 20 steps, every
+    launch shape, with sub-steps and the one-term case (whose launch reads and refreshes fp32(psi))."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 12, 5, capi.EVOLVE_HORNER)
+    E.set_config(*cfg)
+    dt = 0.05 if m > 1 else 0.002
+    E.run(pr, pi, A.rows, dt, 20, sl, m)
+    got = _result(pr, pi)
+    for q in range(5):
+        want = orc.ham_sim(A, P[q], dt * 20, 20, m, substeps=1 << sl)
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, q
+
+
+@pytest.mark.parametrize("layout", [0, 6])
+def test_horner_renormalize(native, layout):
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 10, 4, capi.EVOLVE_HORNER)
+    E.set_config(4, 4 if layout == 0 else 1, layout)
+    E.set_renormalize(True)
+    E.run(pr, pi, A.rows, 0.1, 3, 0, 8)
+    got = _result(pr, pi)
+    assert np.abs(np.linalg.norm(got, axis=1) - 1).max() < 1e-12
+    want = P[2]
+    for _ in range(3):
+        want = orc.ham_sim(A, want, 0.1, 1, 8)
+        want = want / np.linalg.norm(want)
+    assert np.linalg.norm(got[2] - want) < 1e-6
 
 
 def test_autotuner_caches_its_choice(native, tmp_path, monkeypatch):
