@@ -35,7 +35,7 @@ METRIC = "expm(-iHt)·ψ states·steps/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the chosen form's term kernel,
 # from ncu captures (profiles/), keyed by (qubits, states, form, states per block, rows per thread,
 # variant)
-TRAFFIC_PER_LAUNCH = {(20, 8, "mixed", 2, 4, 0): 809.8e6}
+TRAFFIC_PER_LAUNCH = {(20, 8, "mixed", 2, 4, 0): 809.8e6, (20, 8, "horner", 4, 1, 6): 571.6e6}
 
 
 def peaks():
