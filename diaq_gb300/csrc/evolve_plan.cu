@@ -383,28 +383,44 @@ struct EpiHornerIL {
 // D > 0: the matrix values (one float per plane and row) of the next D diagonals are loaded
 // into a register ring ahead of use, so a thread has D HBM reads of the matrix stream in flight
 // and waits on each diagonal only for its state windows (L2 hits, mostly).
-template <class Epi, int D>
+//
+// G states per thread (4 or 8; sp a multiple of G): with 8, one thread takes a whole row of an
+// 8-state block -- one matrix load per row and diagonal, two window vectors per plane.
+//
+// R rows per thread, 256 / (sp/G) rows apart: a block covers R times as many rows, so the state
+// windows of near diagonals (|offset| below the tile) are re-read from L1, and each thread has R
+// independent rows' loads in flight per diagonal.
+template <class Epi, int D, int G = 4, int R = 1>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_il_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                        const float *__restrict__ aim, int64_t rows, const float *__restrict__ xr,
                        const float *__restrict__ xi, Epi epi) {
+    static_assert(G == 4 || G == 8, "4 or 8 states per thread");
+    static_assert(D == 0 || R == 1, "the register ring is for one row per thread");
     __shared__ DiagMeta sm[kMetaChunk];
-    const int sp = epi.sp, quads = sp >> 2;
-    const int64_t t = (int64_t)blockIdx.x * kSpmvThreads + threadIdx.x;
-    const int64_t r = t / quads;
-    const int g = (int)(t - r * quads);
-    float accr[4] = {0.f, 0.f, 0.f, 0.f}, acci[4] = {0.f, 0.f, 0.f, 0.f};
-    auto term = [&](const DiagMeta &m, float a, float b) {
-        const int64_t c = (r + m.off) * sp + 4 * g;
-        const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + c));
-        const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + c));
-        const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
+    const int sp = epi.sp, groups = sp / G;
+    const int per_pass = kSpmvThreads / groups;  // rows one pass of the block covers
+    const int g = (int)threadIdx.x % groups;
+    const int64_t r0 = (int64_t)blockIdx.x * per_pass * R + (int)threadIdx.x / groups;
+    float accr[R][G], acci[R][G];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            accr[q] = fmaf(a, xv[q], accr[q]);
-            accr[q] = fmaf(-b, yv[q], accr[q]);
-            acci[q] = fmaf(a, yv[q], acci[q]);
-            acci[q] = fmaf(b, xv[q], acci[q]);
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+        for (int q = 0; q < G; ++q) accr[j][q] = acci[j][q] = 0.f;
+    auto term = [&](int j, int64_t r, const DiagMeta &m, float a, float b) {
+        const int64_t c = (r + m.off) * sp + G * g;
+#pragma unroll
+        for (int h = 0; h < G / 4; ++h) {
+            const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + c + 4 * h));
+            const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + c + 4 * h));
+            const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                accr[j][4 * h + q] = fmaf(a, xv[q], accr[j][4 * h + q]);
+                accr[j][4 * h + q] = fmaf(-b, yv[q], accr[j][4 * h + q]);
+                acci[j][4 * h + q] = fmaf(a, yv[q], acci[j][4 * h + q]);
+                acci[j][4 * h + q] = fmaf(b, xv[q], acci[j][4 * h + q]);
+            }
         }
     };
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
@@ -412,15 +428,28 @@ __global__ void __launch_bounds__(kSpmvThreads)
         __syncthreads();
         for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
         __syncthreads();
-        if (r >= rows) continue;
+        if (r0 >= rows) continue;
         if constexpr (D == 0) {
-#pragma unroll 4
+#pragma unroll 2
             for (int k = 0; k < cn; ++k) {
-                if (r < sm[k].lo || r >= sm[k].hi) continue;
-                term(sm[k], __ldcs(are + sm[k].base + r), __ldcs(aim + sm[k].base + r));
+                const DiagMeta &m = sm[k];
+                float a[R], b[R];
+#pragma unroll
+                for (int j = 0; j < R; ++j) {  // all R rows' matrix loads first
+                    const int64_t r = r0 + (int64_t)j * per_pass;
+                    const bool in = r < rows && r >= m.lo && r < m.hi;
+                    a[j] = in ? __ldcs(are + m.base + r) : 0.f;
+                    b[j] = in ? __ldcs(aim + m.base + r) : 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    const int64_t r = r0 + (int64_t)j * per_pass;
+                    if (r < rows && r >= m.lo && r < m.hi) term(j, r, m, a[j], b[j]);
+                }
             }
         } else {
             // ring slot d holds diagonal k0 + d; rows outside a diagonal load nothing (value 0)
+            const int64_t r = r0;
             float ra[D], rb[D];
 #pragma unroll
             for (int d = 0; d < D; ++d) {
@@ -438,13 +467,23 @@ __global__ void __launch_bounds__(kSpmvThreads)
                         const bool in = kn < cn && r >= sm[kn].lo && r < sm[kn].hi;
                         ra[d] = in ? __ldcs(are + sm[kn].base + r) : 0.f;
                         rb[d] = in ? __ldcs(aim + sm[kn].base + r) : 0.f;
-                        if (r >= sm[k].lo && r < sm[k].hi) term(sm[k], a, b);
+                        if (r >= sm[k].lo && r < sm[k].hi) term(0, r, sm[k], a, b);
                     }
                 }
             }
         }
     }
-    if (r < rows) epi.apply(r, g, accr, acci);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const int64_t r = r0 + (int64_t)j * per_pass;
+        if (r >= rows) continue;
+#pragma unroll
+        for (int h = 0; h < G / 4; ++h) {  // the epilogue works on quads of states
+            const float ar4[4] = {accr[j][4 * h], accr[j][4 * h + 1], accr[j][4 * h + 2], accr[j][4 * h + 3]};
+            const float ai4[4] = {acci[j][4 * h], acci[j][4 * h + 1], acci[j][4 * h + 2], acci[j][4 * h + 3]};
+            epi.apply(r, g * (G / 4) + h, ar4, ai4);
+        }
+    }
 }
 
 // ---- the plan ------------------------------------------------------------------------------------------
@@ -493,18 +532,33 @@ struct diaq_evolve_s : public diaq_gb300::EvolvePlan {};
 
 namespace diaq_gb300 {
 
-// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4) or 8 (ring of 8).
+// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8), 9 (8
+// states per thread), 10 / 11 (2 / 4 rows per thread), 12 (8 states and 2 rows per thread);
+// 8 states per thread fall back to 4 when the padded state count is not a multiple of 8.
 template <class Epi>
 int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &e) {
-    const int64_t threads = P.n * (P.sp / 4);
-    const unsigned g = (unsigned)((threads + kSpmvThreads - 1) / kSpmvThreads);
+    const int v = P.cfg.pipe;
+    const bool eight = (v == 9 || v == 12) && P.sp % 8 == 0;
+    const int R = v == 10 || v == 12 ? 2 : v == 11 ? 4 : 1;
+    const int64_t rows_per_block = (int64_t)(kSpmvThreads / (P.sp / (eight ? 8 : 4))) * R;
+    const unsigned g = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
     const float *are = (const float *)P.Hc->re, *aim = (const float *)P.Hc->im;
-    if (P.cfg.pipe == 7)
-        dia_spmv_il_kernel<Epi, 4><<<g, kSpmvThreads, 0, P.s>>>(P.Hc->d_meta, P.Hc->nd, are, aim, P.n, xr, xi, e);
-    else if (P.cfg.pipe == 8)
-        dia_spmv_il_kernel<Epi, 8><<<g, kSpmvThreads, 0, P.s>>>(P.Hc->d_meta, P.Hc->nd, are, aim, P.n, xr, xi, e);
+    const DiagMeta *md = P.Hc->d_meta;
+    const int nd = P.Hc->nd;
+    if (eight && R == 2)
+        dia_spmv_il_kernel<Epi, 0, 8, 2><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+    else if (eight)
+        dia_spmv_il_kernel<Epi, 0, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+    else if (R == 2)
+        dia_spmv_il_kernel<Epi, 0, 4, 2><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+    else if (R == 4)
+        dia_spmv_il_kernel<Epi, 0, 4, 4><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+    else if (v == 7)
+        dia_spmv_il_kernel<Epi, 4><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+    else if (v == 8)
+        dia_spmv_il_kernel<Epi, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
     else
-        dia_spmv_il_kernel<Epi, 0><<<g, kSpmvThreads, 0, P.s>>>(P.Hc->d_meta, P.Hc->nd, are, aim, P.n, xr, xi, e);
+        dia_spmv_il_kernel<Epi, 0><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;
 }
@@ -783,7 +837,8 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
                 {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
                 {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
-                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}};
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}, {4, 1, 10},
+                {4, 1, 11}, {4, 1, 12}};
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -926,9 +981,9 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_block < 1 || states_per_block > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_block in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
-        if (pipelined < 0 || pipelined > 8 || pipelined == 5)
+        if (pipelined < 0 || pipelined > 12 || pipelined == 5)
             return set_error(DIAQ_ERR_INVALID, "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), "
-                                               "4 (shuffled windows), 6, 7, 8 (interleaved states)");
+                                               "4 (shuffled windows), 6-12 (interleaved states)");
         if (pipelined >= 6) {
             if (!(f32 && states_per_block == 4 && rows_per_thread == 1))
                 return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernel is the mixed mode's, 4 states and "
