@@ -387,9 +387,10 @@ struct EpiHornerIL {
 // G states per thread (4 or 8; sp a multiple of G): with 8, one thread takes a whole row of an
 // 8-state block -- one matrix load per row and diagonal, two window vectors per plane.
 //
-// R rows per thread, 256 / (sp/G) rows apart: a block covers R times as many rows, so the state
-// windows of near diagonals (|offset| below the tile) are re-read from L1, and each thread has R
-// independent rows' loads in flight per diagonal.
+// R rows per thread, 256 / (sp/G) rows apart, widen a block's tile so that the state windows of
+// near diagonals come back from L1, with R independent rows' loads in flight per diagonal.  On the
+// 20-qubit chain, 8 states, Horner: R = 2 and 4 measured 3.40 and 3.89 ms per step against 2.53
+// for R = 1 (more registers, fewer warps), so the plans launch R = 1 only.
 template <class Epi, int D, int G = 4, int R = 1>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_il_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
@@ -532,27 +533,19 @@ struct diaq_evolve_s : public diaq_gb300::EvolvePlan {};
 
 namespace diaq_gb300 {
 
-// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8), 9 (8
-// states per thread), 10 / 11 (2 / 4 rows per thread), 12 (8 states and 2 rows per thread);
-// 8 states per thread fall back to 4 when the padded state count is not a multiple of 8.
+// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8) or 9 (8
+// states per thread; 4 when the padded state count is not a multiple of 8).
 template <class Epi>
 int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &e) {
     const int v = P.cfg.pipe;
-    const bool eight = (v == 9 || v == 12) && P.sp % 8 == 0;
-    const int R = v == 10 || v == 12 ? 2 : v == 11 ? 4 : 1;
-    const int64_t rows_per_block = (int64_t)(kSpmvThreads / (P.sp / (eight ? 8 : 4))) * R;
+    const bool eight = v == 9 && P.sp % 8 == 0;
+    const int64_t rows_per_block = kSpmvThreads / (P.sp / (eight ? 8 : 4));
     const unsigned g = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
     const float *are = (const float *)P.Hc->re, *aim = (const float *)P.Hc->im;
     const DiagMeta *md = P.Hc->d_meta;
     const int nd = P.Hc->nd;
-    if (eight && R == 2)
-        dia_spmv_il_kernel<Epi, 0, 8, 2><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
-    else if (eight)
+    if (eight)
         dia_spmv_il_kernel<Epi, 0, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
-    else if (R == 2)
-        dia_spmv_il_kernel<Epi, 0, 4, 2><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
-    else if (R == 4)
-        dia_spmv_il_kernel<Epi, 0, 4, 4><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
     else if (v == 7)
         dia_spmv_il_kernel<Epi, 4><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
     else if (v == 8)
@@ -837,8 +830,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
                 {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
                 {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
-                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}, {4, 1, 10},
-                {4, 1, 11}, {4, 1, 12}};
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}};
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -981,9 +973,9 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_block < 1 || states_per_block > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_block in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
-        if (pipelined < 0 || pipelined > 12 || pipelined == 5)
+        if (pipelined < 0 || pipelined > 9 || pipelined == 5)
             return set_error(DIAQ_ERR_INVALID, "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), "
-                                               "4 (shuffled windows), 6-12 (interleaved states)");
+                                               "4 (shuffled windows), 6-9 (interleaved states)");
         if (pipelined >= 6) {
             if (!(f32 && states_per_block == 4 && rows_per_thread == 1))
                 return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernel is the mixed mode's, 4 states and "
