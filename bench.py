@@ -649,7 +649,10 @@ def run_ours(args, rank, world):
     achieved = step_bytes / (ms / K * 1e-3) / 1e9
     k_launch, v_launch = chosen.config()
     variant = chosen.pipelined()
-    kernel = (f"dia_spmv_il_kernel<EpiHornerIL,{[0, 4, 8][variant - 6]}>" if variant >= 6 else
+    il_names = {6: "dia_spmv_il_kernel<EpiHornerIL,0,4>", 7: "dia_spmv_il_kernel<EpiHornerIL,4,4>",
+                8: "dia_spmv_il_kernel<EpiHornerIL,8,4>", 9: "dia_spmv_il_kernel<EpiHornerIL,0,8>",
+                10: "dia_spmv_il_kernel<EpiHornerIL,0,8,1,6>"}
+    kernel = (il_names.get(variant) if variant >= 6 else
               f"dia_spmv_kernel<float,{k_launch},{v_launch},EpiHorner>" if variant == 0 else
               f"variant {variant}, {k_launch} states x {v_launch} rows per thread")
     # DRAM bytes of one launch from the ncu capture of this workload, form and shape (profiles/);
