@@ -395,7 +395,7 @@ def run_batched(args):
     mine = partition_instances([k * (2 * n + 1) * (1 << n) for _, n, k, _ in specs], world)[rank]
     specs = [specs[i] for i in mine]
     dt, tol = 0.02, TOL_STEP
-    out = {"mode": "batched", "instances": args.instances, "n_range": [args.n_lo, args.n_hi], "dt": dt,
+    out = {"mode": "batched", "horner": args.horner, "instances": args.instances, "n_range": [args.n_lo, args.n_hi], "dt": dt,
            "states": all_states, "n_gpus": world, "scaling": "weak" if world > 1 else None, "variants": {}}
     for variant in (["c64", "c128"] if args.variant == "both" else [args.variant]):
         prec = capi.C64 if variant == "c64" else capi.C128
@@ -432,6 +432,7 @@ def run_batched(args):
             small = [j for j, idx in enumerate(grp) if specs[idx][1] <= 12][:3]
             start = {j: (prs[j][0].cpu().numpy() + 1j * pis[j][0].cpu().numpy()) for j in small}
             B = capi.Batch(mats, prs, pis)
+            B.set_horner(args.horner)
             if variant == "c128":
                 B.set_config(4, 2)   # FP64-bound either way; autotuning would cost minutes of steps
             stream = torch.cuda.current_stream()
@@ -650,8 +651,7 @@ def run_ours(args, rank, world):
     k_launch, v_launch = chosen.config()
     variant = chosen.pipelined()
     il_names = {6: "dia_spmv_il_kernel<EpiHornerIL,0,4>", 7: "dia_spmv_il_kernel<EpiHornerIL,4,4>",
-                8: "dia_spmv_il_kernel<EpiHornerIL,8,4>", 9: "dia_spmv_il_kernel<EpiHornerIL,0,8>",
-                10: "dia_spmv_il_kernel<EpiHornerIL,0,8,1,6>"}
+                8: "dia_spmv_il_kernel<EpiHornerIL,8,4>", 9: "dia_spmv_il_kernel<EpiHornerIL,0,8>"}
     kernel = (il_names.get(variant) if variant >= 6 else
               f"dia_spmv_kernel<float,{k_launch},{v_launch},EpiHorner>" if variant == 0 else
               f"variant {variant}, {k_launch} states x {v_launch} rows per thread")
@@ -710,7 +710,8 @@ def main():
     ap.add_argument("--spmv-reps", type=int, default=1000)
     ap.add_argument("--states", type=int, default=8, help="states evolved together by the chosen form")
     ap.add_argument("--shape", default="", help="chosen mode: force the launch shape 'states,rows,pipelined'")
-    ap.add_argument("--horner", action="store_true", help="chosen mode: Horner-form evaluation (DIAQ_EVOLVE_HORNER)")
+    ap.add_argument("--horner", action="store_true",
+                    help="chosen and batched modes: Horner-form evaluation (DIAQ_EVOLVE_HORNER, diaq_batch_set_horner)")
     ap.add_argument("--instances", type=int, default=512, help="batched mode: Hamiltonians")
     ap.add_argument("--n-lo", type=int, default=10)
     ap.add_argument("--n-hi", type=int, default=22)

@@ -67,6 +67,7 @@ SIGNATURES = {
     "diaq_batch_run": (INT, [P, F64, P, P, I64, P]),
     "diaq_batch_set_config": (INT, [P, INT, INT]),
     "diaq_batch_config": (INT, [P, P, P, P]),
+    "diaq_batch_set_horner": (INT, [P, INT]),
     "diaq_mlp_num_params": (INT, []),
     "diaq_mlp_create": (INT, [ctypes.c_uint64, P]),
     "diaq_mlp_destroy": (INT, [P]),
@@ -324,6 +325,9 @@ class Batch:
 
     def set_config(self, states_per_launch: int, rows_per_thread: int = 0):
         check(lib().diaq_batch_set_config(self.h, states_per_launch, rows_per_thread))
+
+    def set_horner(self, on: bool = True):
+        check(lib().diaq_batch_set_horner(self.h, 1 if on else 0))
 
     def config(self):
         k, v, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

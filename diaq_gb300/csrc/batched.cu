@@ -15,6 +15,11 @@
 //   last term of a sub-step:    psi += hi + lo in float64, and v <- T(psi) for the next one.
 // The term vectors ping-pong between two buffers; when an instance's step has an odd number of
 // launches, one extra phase copies its first input back into place.
+//
+// Horner form (diaq_batch_set_horner, instances with m >= 2): w_m = psi, w_k = T(psi) +
+// (-i tau/(k+1)) H w_{k+1}, psi += (-i tau) H w_1 in float64 -- no running sum.  T(psi) stays in
+// v_a for the whole sub-step (the last term refreshes it), w alternates between v_b and the
+// otherwise unused hi vectors, and no copy phase is needed.
 #include <sys/stat.h>
 
 #include <algorithm>
@@ -38,6 +43,7 @@ struct BatchInst {
     int nd, nrhs;
     int m, phases;   // Taylor terms per sub-step; launches per step (2^s m, +1 when odd)
     int sub;         // 2^s
+    int horner;      // Horner evaluation (m >= 2 and the batch's form)
     double tau;      // dt / 2^s
     double *pr, *pi; // states, leading dimension rows
     void *var, *vai, *vbr, *vbi, *hr, *hi, *lr, *li;  // T work vectors, leading dimension rows
@@ -97,10 +103,19 @@ __global__ void __launch_bounds__(kSpmvThreads)
         }
         const int k = phase % I.m + 1;
         const bool first = (k == 1), last = (k == I.m);
-        const T *xr = (const T *)((phase & 1) ? I.vbr : I.var);
-        const T *xi = (const T *)((phase & 1) ? I.vbi : I.vai);
-        T *outr = (T *)((phase & 1) ? I.var : I.vbr);
-        T *outi = (T *)((phase & 1) ? I.vai : I.vbi);
+        const T *xr, *xi;
+        T *outr, *outi;
+        if (I.horner) {  // x: T(psi) for the first term, else the previous term's w
+            xr = (const T *)(first ? I.var : ((k - 1) & 1) ? I.vbr : I.hr);
+            xi = (const T *)(first ? I.vai : ((k - 1) & 1) ? I.vbi : I.hi);
+            outr = (T *)((k & 1) ? I.vbr : I.hr);
+            outi = (T *)((k & 1) ? I.vbi : I.hi);
+        } else {
+            xr = (const T *)((phase & 1) ? I.vbr : I.var);
+            xi = (const T *)((phase & 1) ? I.vbi : I.vai);
+            outr = (T *)((phase & 1) ? I.var : I.vbr);
+            outi = (T *)((phase & 1) ? I.vai : I.vbi);
+        }
         xr += (int64_t)q0 * ld;
         xi += (int64_t)q0 * ld;
 
@@ -156,6 +171,32 @@ __global__ void __launch_bounds__(kSpmvThreads)
             }
         }
         if (r0 >= I.rows) continue;
+        if (I.horner) {
+            const T scale = (T)(I.tau / (double)(I.m - k + 1));
+            T *fr = (T *)I.var, *fi = (T *)I.vai;
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                if (q >= kq) break;
+#pragma unroll
+                for (int v = 0; v < VR; ++v) {
+                    const int64_t r = r0 + v;
+                    if (r >= I.rows) continue;
+                    const int64_t i = (int64_t)(q0 + q) * ld + r;
+                    const T tr = acci[q][v] * scale, ti = -accr[q][v] * scale;
+                    if (!last) {
+                        outr[i] = fr[i] + tr;
+                        outi[i] = fi[i] + ti;
+                    } else {  // this launch reads w_1, not T(psi): refreshing it here is safe
+                        const double nr = I.pr[i] + (double)tr, ni = I.pi[i] + (double)ti;
+                        I.pr[i] = nr;
+                        I.pi[i] = ni;
+                        fr[i] = (T)nr;
+                        fi[i] = (T)ni;
+                    }
+                }
+            }
+            continue;
+        }
         const T scale = (T)(I.tau / (double)k);
         T *hr = (T *)I.hr, *hi_ = (T *)I.hi, *lr = (T *)I.lr, *li = (T *)I.li;
 #pragma unroll
@@ -216,6 +257,7 @@ struct Batch {
     std::vector<int> graph_key;       // (s_i, m_i) of the recorded graph, plus dt bits
     double graph_dt = 0.0;
     int max_phases = 0;
+    bool horner = false;              // Horner evaluation for instances with m >= 2
     ~Batch() {
         if (graph) cudaGraphExecDestroy(graph);
         cudaFree(d_inst);
@@ -307,8 +349,9 @@ static int set_schedule(Batch &B, double dt, const int *sl, const int *m) {
         I.sub = 1 << sl[i];
         I.m = m[i];
         I.tau = dt / (double)I.sub;
+        I.horner = B.horner && I.m >= 2;
         const int launches = I.sub * I.m;
-        I.phases = launches + (launches & 1);
+        I.phases = I.horner ? launches : launches + (launches & 1);
         B.max_phases = std::max(B.max_phases, I.phases);
     }
     DQ_CUDA(cudaMemcpy(B.d_inst, B.inst.data(), sizeof(BatchInst) * B.inst.size(), cudaMemcpyHostToDevice));
@@ -388,9 +431,9 @@ static std::string batch_key(const Batch &B) {
     for (auto &ch : name)
         if (ch == '"' || ch == ' ') ch = '_';
     char buf[256];
-    std::snprintf(buf, sizeof(buf), "%s|batch|%s|inst=%zu|rows=%lld|staterows=%lld|phases=%d", name.c_str(),
-                  B.prec == DIAQ_C64 ? "c64" : "c128", B.inst.size(), (long long)rows, (long long)states,
-                  B.max_phases);
+    std::snprintf(buf, sizeof(buf), "%s|batch|%s%s|inst=%zu|rows=%lld|staterows=%lld|phases=%d", name.c_str(),
+                  B.prec == DIAQ_C64 ? "c64" : "c128", B.horner ? "|horner" : "", B.inst.size(), (long long)rows,
+                  (long long)states, B.max_phases);
     return buf;
 }
 
@@ -537,6 +580,16 @@ int diaq_batch_set_config(diaq_batch_t B, int states_per_launch, int rows_per_th
     }
     if (B->graph) cudaGraphExecDestroy(B->graph);
     B->graph = nullptr;
+    return DIAQ_OK;
+}
+
+int diaq_batch_set_horner(diaq_batch_t B, int on) {
+    if (!B) return set_error(DIAQ_ERR_INVALID, "batch is NULL");
+    if (B->horner != (on != 0)) {
+        B->horner = on != 0;
+        if (B->graph) cudaGraphExecDestroy(B->graph);
+        B->graph = nullptr;  // the schedule (phases per instance) is rebuilt on the next run
+    }
     return DIAQ_OK;
 }
 

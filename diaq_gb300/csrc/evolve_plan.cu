@@ -392,9 +392,10 @@ struct EpiHornerIL {
 // 20-qubit chain, 8 states, Horner: R = 2 and 4 measured 3.40 and 3.89 ms per step against 2.53
 // for R = 1 (more registers, fewer warps), so the plans launch R = 1 only.
 //
-// MINB > 1 asks the compiler for at least that many blocks per SM (fewer registers, some spill).
-template <class Epi, int D, int G = 4, int R = 1, int MINB = 1>
-__global__ void __launch_bounds__(kSpmvThreads, MINB)
+// A six-blocks-per-SM launch bound on the 8-state kernel (40 registers, a little spill) measured
+// slower, 3.05 against 2.62 ms per step.
+template <class Epi, int D, int G = 4, int R = 1>
+__global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_il_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                        const float *__restrict__ aim, int64_t rows, const float *__restrict__ xr,
                        const float *__restrict__ xi, Epi epi) {
@@ -535,21 +536,18 @@ struct diaq_evolve_s : public diaq_gb300::EvolvePlan {};
 
 namespace diaq_gb300 {
 
-// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8), 9 (8
-// states per thread; 4 when the padded state count is not a multiple of 8) or 10 (as 9, at
-// least 6 blocks per SM).
+// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8) or 9 (8
+// states per thread; 4 when the padded state count is not a multiple of 8).
 template <class Epi>
 int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &e) {
     const int v = P.cfg.pipe;
-    const bool eight = (v == 9 || v == 10) && P.sp % 8 == 0;
+    const bool eight = v == 9 && P.sp % 8 == 0;
     const int64_t rows_per_block = kSpmvThreads / (P.sp / (eight ? 8 : 4));
     const unsigned g = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
     const float *are = (const float *)P.Hc->re, *aim = (const float *)P.Hc->im;
     const DiagMeta *md = P.Hc->d_meta;
     const int nd = P.Hc->nd;
-    if (eight && v == 10)
-        dia_spmv_il_kernel<Epi, 0, 8, 1, 6><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
-    else if (eight)
+    if (eight)
         dia_spmv_il_kernel<Epi, 0, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
     else if (v == 7)
         dia_spmv_il_kernel<Epi, 4><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
@@ -835,7 +833,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
                 {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
                 {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
-                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}, {4, 1, 10}};
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}};
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -978,9 +976,9 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_block < 1 || states_per_block > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_block in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
-        if (pipelined < 0 || pipelined > 10 || pipelined == 5)
+        if (pipelined < 0 || pipelined > 9 || pipelined == 5)
             return set_error(DIAQ_ERR_INVALID, "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), "
-                                               "4 (shuffled windows), 6-10 (interleaved states)");
+                                               "4 (shuffled windows), 6-9 (interleaved states)");
         if (pipelined >= 6) {
             if (!(f32 && states_per_block == 4 && rows_per_thread == 1))
                 return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernel is the mixed mode's, 4 states and "

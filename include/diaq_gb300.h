@@ -257,7 +257,7 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
  * windows as aligned vectors shifted across lanes and prefetch the matrix into L2 4 / 8 / 0
  * diagonals ahead; for the float32 modes with (4 states, 1 row), 6 / 7 / 8 keep the work vectors
  * interleaved per row (any window one aligned vector) and load the matrix 0 / 4 / 8 diagonals
- * ahead into registers, 9 with 8 states per thread, 10 as 9 with at least 6 blocks per SM.
+ * ahead into registers, 9 with 8 states per thread.
  * 0 states = choose automatically: on the first run the autotuner times the candidate shapes on
  * two steps of scratch copies of the states and keeps the fastest, caching the choice in a JSON
  * file (DIAQ_AUTOTUNE_CACHE, else $HOME/.cache/diaq_gb300/autotune.json).  Setting a shape drops
@@ -313,6 +313,12 @@ int diaq_batch_run(diaq_batch_t B, double dt, const int *substeps_log2, const in
  * 0 states for automatic; and read back the shape and the phases per step. */
 int diaq_batch_set_config(diaq_batch_t B, int states_per_launch, int rows_per_thread);
 int diaq_batch_config(diaq_batch_t B, int *states_per_launch, int *rows_per_thread, int *phases_per_step);
+
+/* on != 0: evaluate the Taylor polynomial of instances with m >= 2 in Horner form (as
+ * DIAQ_EVOLVE_HORNER: w_k = psi + A w_{k+1} / (k+1) in the batch's precision, the last step in
+ * float64), no running sum and no copy phase; off (the compensated forward sum) by default.
+ * Drops the recorded step. */
+int diaq_batch_set_horner(diaq_batch_t B, int on);
 
 /* ------------------------------------------------------------------------------------------
  * The learned (s, m) proposer: an FP32 MLP 16 -> 64 -> 64 -> 21 + 30 logits (ReLU), trained

@@ -47,6 +47,31 @@ def test_batched_matches_oracle(native, precision, tol):
     assert phases == max((1 << si) * mi + ((1 << si) * mi) % 2 for si, mi in zip(s, m))
 
 
+@pytest.mark.parametrize("precision,tol", [(1, 1e-6), (0, 1e-12)])
+def test_batched_horner_matches_oracle(native, precision, tol):
+    """The Horner form in the batch: instances with m >= 2 evaluate from the inside out, the
+    m = 1 instance keeps the compensated path; no copy phase for the Horner instances."""
+    import torch
+
+    capi, _ = native
+    mats, oms, prs, pis, P0 = _make(capi, SPECS, precision)
+    B = capi.Batch(mats, prs, pis)
+    B.set_horner(True)
+    s = [0, 1, 0, 2, 0]
+    m = [11, 8, 13, 6, 1]
+    dts = [0.02, 0.02, 0.02, 0.02, 0.02]
+    B.run(0.02, s, m, 4)
+    torch.cuda.synchronize()
+    for i, A in enumerate(oms):
+        got = (prs[i] + 1j * pis[i]).cpu().numpy()
+        for q in range(P0[i].shape[0]):
+            want = orc.ham_sim(A, P0[i][q], 4 * dts[i], 4, m[i], substeps=1 << s[i])
+            err = np.linalg.norm(got[q] - want) / np.linalg.norm(want)
+            assert err < (tol if m[i] > 1 else max(tol, 1e-6)), (i, q, err)
+    _, _, phases = B.config()
+    assert phases == max((1 << si) * mi + (((1 << si) * mi) % 2 if mi == 1 else 0) for si, mi in zip(s, m))
+
+
 @pytest.mark.parametrize("cfg", [(8, 1), (8, 2), (4, 4), (2, 4), (1, 4), (1, 1)])
 def test_batched_every_launch_shape(native, cfg):
     import torch
