@@ -35,7 +35,8 @@ METRIC = "expm(-iHt)·ψ states·steps/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the chosen form's term kernel,
 # from ncu captures (profiles/), keyed by (qubits, states, form, states per block, rows per thread,
 # variant)
-TRAFFIC_PER_LAUNCH = {(20, 8, "mixed", 2, 4, 0): 809.8e6, (20, 8, "horner", 4, 1, 6): 571.6e6}
+TRAFFIC_PER_LAUNCH = {(20, 8, "mixed", 2, 4, 0): 809.8e6, (20, 8, "horner", 4, 1, 6): 571.6e6,
+                      (20, 8, "horner", 4, 1, 9): 555.1e6}
 
 
 def peaks():
@@ -580,6 +581,16 @@ def run_ours(args, rank, world):
     lps = chosen.launches_per_step()
     launches = K * lps + 2
 
+    # ---- the chosen form on one state (config 2 evolves a single psi) ----
+    one = capi.Evolve(H, 1, CHOSEN_MODE)
+    o_r = torch.from_numpy(np.ascontiguousarray(P0[0].real)).to(dev)
+    o_i = torch.from_numpy(np.ascontiguousarray(P0[0].imag)).to(dev)
+    one.run(o_r, o_i, N, DT, W, s_c, m_c, sp)
+    torch.cuda.synchronize()
+    ms_one = _timed(stream, lambda: one.run(o_r, o_i, N, DT, K, s_c, m_c, sp))
+    one_shape = list(one.config()) + [one.pipelined()]
+    del one, o_r, o_i
+
     # ---- accuracy of the chosen form: the same W + K steps in c128 at a tight tolerance ----
     s_r, m_r = capi.select_sm(norm1.value, DT, 1e-14, 1.0, 100)
     refp = capi.Evolve(H, S, capi.EVOLVE_C128)
@@ -674,6 +685,9 @@ def run_ours(args, rank, world):
                    "parallelism": f"replicas{world}"},
         "accuracy": {"rel_err_max": float(errs.max()), "fidelity_min": float(fid.min()),
                      "vs": f"c128 evolution at tol 1e-14 ({1 << s_r}x{m_r} terms/step)", "steps": W + K},
+        "chosen_one_state": {"value": world * K / (ms_one / 1e3), "ms_per_step": ms_one / K,
+                             "launch_shape": one_shape,
+                             "speedup_over_plain": (world * K / (ms_one / 1e3)) / plain_value},
         "plain": {"value": plain_value, "ms_per_step": ms_plain / K, "substeps": 1 << s_p, "taylor_terms": m_p,
                   "launches_per_step": lps_plain, "speedup_chosen_over_plain": value / plain_value},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
