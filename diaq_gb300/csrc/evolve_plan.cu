@@ -199,6 +199,12 @@ struct EpiHorner {
     }
 };
 
+// Index of the float4 holding states 4 quad .. 4 quad + 3 of row r in the tiled interleaved layout
+// (quads = sp / 4; see the interleaved kernels below).
+__device__ __forceinline__ int64_t il_at(int64_t r, int quad, int quads) {
+    return ((r >> 5) * quads + quad) * 128 + ((r & 31) << 2);
+}
+
 // Renormalisation in float64: per state, partial sums of |psi|^2 over row blocks (fixed order),
 // then every block sums its state's partials and scales its rows; in the mixed mode it also
 // refreshes the float32 copy the next step starts from.
@@ -238,8 +244,8 @@ __global__ void renorm_kernel(double *__restrict__ pr, double *__restrict__ pi, 
         const double x = a[i] * c, y = b[i] * c;
         a[i] = x;
         b[i] = y;
-        if (fr) {  // the float32 copy: planar (sp = 0) or interleaved
-            const int64_t j = sp ? i * sp + q : (int64_t)q * n + i;
+        if (fr) {  // the float32 copy: planar (sp = 0) or tiled interleaved
+            const int64_t j = sp ? il_at(i, q >> 2, sp >> 2) + (q & 3) : (int64_t)q * n + i;
             fr[j] = (float)x;
             fi[j] = (float)y;
         }
@@ -251,24 +257,32 @@ __global__ void to_f32_kernel(const double *__restrict__ a, float *__restrict__ 
         b[i] = (float)a[i];
 }
 
-// ---- interleaved states (kernel variant 6) ----------------------------------------------------------
-// The float32 work vectors of the mixed mode hold the states interleaved per row: element (r, q)
-// at v[r * sp + q], sp = nrhs rounded up to a multiple of 4 (the padding states are zero).  A
-// state window at any diagonal offset is then sp contiguous floats per row, 16-byte aligned, so
-// every thread reads four states of one row with one vector load per array, whatever the offset
-// (the planar layout splits the windows of offsets that are not multiples of 4).  Thread t owns
-// row t / (sp/4) and states 4 (t mod sp/4) .. +3; the threads of a row share the matrix value
-// (an L1 broadcast).  Few registers per thread: 8 blocks of 256 threads fit on an SM.
+// ---- interleaved states (kernel variants 6-9) -------------------------------------------------------
+// The float32 work vectors of the float32 modes can hold the states interleaved in tiles: rows in
+// blocks of 32, and within a block each quad of 4 states stored as 32 rows x 4 floats (512
+// bytes).  Element (r, q) sits at ((r / 32) * (sp / 4) + q / 4) * 128 + (r mod 32) * 4 + q mod 4,
+// sp = nrhs rounded up to a power of two >= 4 (at most 32; the padding states are zero) and the
+// rows padded to a multiple of 32.  A warp works on 32 consecutive rows and one or two quads: its
+// state window at any diagonal offset is one or two contiguous 512-byte runs (one 16-byte load
+// per lane and quad), its matrix values 128 contiguous bytes, and its epilogue reads and writes
+// contiguous quads too.  (The planar layout splits the windows of offsets that are not multiples
+// of 4; a row-major interleave spreads a warp's window over sp * 128 bytes.)
 
-// psi (state q at p[q * ld + r]) -> interleaved float32, padding states zero.
+// psi (state q at p[q * ld + r]) -> tiled float32, padding states and rows zero.
 __global__ void to_f32_il_kernel(const double *__restrict__ pr, const double *__restrict__ pi, int64_t ld,
-                                 int64_t n, int nrhs, int sp, float *__restrict__ fr, float *__restrict__ fi) {
-    const int64_t cnt = n * sp;
+                                 int64_t n, int64_t n_pad, int nrhs, int sp, float *__restrict__ fr,
+                                 float *__restrict__ fi) {
+    const int64_t cnt = n_pad * sp;
+    const int quads = sp >> 2;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = e / sp;
-        const int q = (int)(e - r * sp);
-        fr[e] = q < nrhs ? (float)pr[q * ld + r] : 0.f;
-        fi[e] = q < nrhs ? (float)pi[q * ld + r] : 0.f;
+        const int64_t blk = e / (quads * 128);
+        const int rem = (int)(e - blk * quads * 128);
+        const int quad = rem >> 7, lr = (rem & 127) >> 2, c = rem & 3;
+        const int64_t r = blk * 32 + lr;
+        const int q = quad * 4 + c;
+        const bool live = r < n && q < nrhs;
+        fr[e] = live ? (float)pr[q * ld + r] : 0.f;
+        fi[e] = live ? (float)pi[q * ld + r] : 0.f;
     }
 }
 
@@ -282,7 +296,7 @@ struct EpiMixedIL {
     float scale;
     int first, last;
     __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
-        const int64_t i = r * sp + 4 * g;
+        const int64_t i = il_at(r, g, sp >> 2);
         float tr[4], ti[4], h_r[4], h_i[4], l_r[4], l_i[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -349,7 +363,7 @@ struct EpiHornerIL {
     float scale;
     int last;
     __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
-        const int64_t i = r * sp + 4 * g;
+        const int64_t i = il_at(r, g, sp >> 2);
         float tr[4], ti[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -380,50 +394,44 @@ struct EpiHornerIL {
     }
 };
 
+// Thread mapping: warp w of a block takes quad group g = w mod (sp/G) of the 32 rows of row
+// block (block * 8 / (sp/G) + w / (sp/G)); lane l takes row 32 * (that row block) + l.
+//
 // D > 0: the matrix values (one float per plane and row) of the next D diagonals are loaded
 // into a register ring ahead of use, so a thread has D HBM reads of the matrix stream in flight
 // and waits on each diagonal only for its state windows (L2 hits, mostly).
 //
-// G states per thread (4 or 8; sp a multiple of G): with 8, one thread takes a whole row of an
-// 8-state block -- one matrix load per row and diagonal, two window vectors per plane.
-//
-// R rows per thread, 256 / (sp/G) rows apart, widen a block's tile so that the state windows of
-// near diagonals come back from L1, with R independent rows' loads in flight per diagonal.  On the
-// 20-qubit chain, 8 states, Horner: R = 2 and 4 measured 3.40 and 3.89 ms per step against 2.53
-// for R = 1 (more registers, fewer warps), so the plans launch R = 1 only.
-//
-// A six-blocks-per-SM launch bound on the 8-state kernel (40 registers, a little spill) measured
-// slower, 3.05 against 2.62 ms per step.
-template <class Epi, int D, int G = 4, int R = 1>
+// G states per thread (4 or 8; sp a multiple of G): with 8, a warp covers 8 states of its rows --
+// one matrix load per row and diagonal, two window vectors per plane.  (Several rows per thread,
+// for a wider tile, measured slower: 2.86-3.89 ms per step against 2.53 on the 20-qubit chain.)
+template <class Epi, int D, int G = 4>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_il_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                        const float *__restrict__ aim, int64_t rows, const float *__restrict__ xr,
                        const float *__restrict__ xi, Epi epi) {
     static_assert(G == 4 || G == 8, "4 or 8 states per thread");
-    static_assert(D == 0 || R == 1, "the register ring is for one row per thread");
     __shared__ DiagMeta sm[kMetaChunk];
-    const int sp = epi.sp, groups = sp / G;
-    const int per_pass = kSpmvThreads / groups;  // rows one pass of the block covers
-    const int g = (int)threadIdx.x % groups;
-    const int64_t r0 = (int64_t)blockIdx.x * per_pass * R + (int)threadIdx.x / groups;
-    float accr[R][G], acci[R][G];
+    const int quads = epi.sp >> 2, groups = epi.sp / G;
+    const int wid = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    const int g = wid % groups;
+    const int64_t r = ((int64_t)blockIdx.x * (8 / groups) + wid / groups) * 32 + lane;
+    float accr[G], acci[G];
 #pragma unroll
-    for (int j = 0; j < R; ++j)
-#pragma unroll
-        for (int q = 0; q < G; ++q) accr[j][q] = acci[j][q] = 0.f;
-    auto term = [&](int j, int64_t r, const DiagMeta &m, float a, float b) {
-        const int64_t c = (r + m.off) * sp + G * g;
+    for (int q = 0; q < G; ++q) accr[q] = acci[q] = 0.f;
+    auto term = [&](const DiagMeta &m, float a, float b) {
+        const int64_t c = r + m.off;
 #pragma unroll
         for (int h = 0; h < G / 4; ++h) {
-            const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + c + 4 * h));
-            const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + c + 4 * h));
+            const int64_t at = il_at(c, g * (G / 4) + h, quads);
+            const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + at));
+            const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + at));
             const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                accr[j][4 * h + q] = fmaf(a, xv[q], accr[j][4 * h + q]);
-                accr[j][4 * h + q] = fmaf(-b, yv[q], accr[j][4 * h + q]);
-                acci[j][4 * h + q] = fmaf(a, yv[q], acci[j][4 * h + q]);
-                acci[j][4 * h + q] = fmaf(b, xv[q], acci[j][4 * h + q]);
+                accr[4 * h + q] = fmaf(a, xv[q], accr[4 * h + q]);
+                accr[4 * h + q] = fmaf(-b, yv[q], accr[4 * h + q]);
+                acci[4 * h + q] = fmaf(a, yv[q], acci[4 * h + q]);
+                acci[4 * h + q] = fmaf(b, xv[q], acci[4 * h + q]);
             }
         }
     };
@@ -432,28 +440,15 @@ __global__ void __launch_bounds__(kSpmvThreads)
         __syncthreads();
         for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
         __syncthreads();
-        if (r0 >= rows) continue;
+        if (r >= rows) continue;
         if constexpr (D == 0) {
-#pragma unroll 2
+#pragma unroll 4
             for (int k = 0; k < cn; ++k) {
-                const DiagMeta &m = sm[k];
-                float a[R], b[R];
-#pragma unroll
-                for (int j = 0; j < R; ++j) {  // all R rows' matrix loads first
-                    const int64_t r = r0 + (int64_t)j * per_pass;
-                    const bool in = r < rows && r >= m.lo && r < m.hi;
-                    a[j] = in ? __ldcs(are + m.base + r) : 0.f;
-                    b[j] = in ? __ldcs(aim + m.base + r) : 0.f;
-                }
-#pragma unroll
-                for (int j = 0; j < R; ++j) {
-                    const int64_t r = r0 + (int64_t)j * per_pass;
-                    if (r < rows && r >= m.lo && r < m.hi) term(j, r, m, a[j], b[j]);
-                }
+                if (r < sm[k].lo || r >= sm[k].hi) continue;
+                term(sm[k], __ldcs(are + sm[k].base + r), __ldcs(aim + sm[k].base + r));
             }
         } else {
             // ring slot d holds diagonal k0 + d; rows outside a diagonal load nothing (value 0)
-            const int64_t r = r0;
             float ra[D], rb[D];
 #pragma unroll
             for (int d = 0; d < D; ++d) {
@@ -471,22 +466,18 @@ __global__ void __launch_bounds__(kSpmvThreads)
                         const bool in = kn < cn && r >= sm[kn].lo && r < sm[kn].hi;
                         ra[d] = in ? __ldcs(are + sm[kn].base + r) : 0.f;
                         rb[d] = in ? __ldcs(aim + sm[kn].base + r) : 0.f;
-                        if (r >= sm[k].lo && r < sm[k].hi) term(0, r, sm[k], a, b);
+                        if (r >= sm[k].lo && r < sm[k].hi) term(sm[k], a, b);
                     }
                 }
             }
         }
     }
+    if (r >= rows) return;
 #pragma unroll
-    for (int j = 0; j < R; ++j) {
-        const int64_t r = r0 + (int64_t)j * per_pass;
-        if (r >= rows) continue;
-#pragma unroll
-        for (int h = 0; h < G / 4; ++h) {  // the epilogue works on quads of states
-            const float ar4[4] = {accr[j][4 * h], accr[j][4 * h + 1], accr[j][4 * h + 2], accr[j][4 * h + 3]};
-            const float ai4[4] = {acci[j][4 * h], acci[j][4 * h + 1], acci[j][4 * h + 2], acci[j][4 * h + 3]};
-            epi.apply(r, g * (G / 4) + h, ar4, ai4);
-        }
+    for (int h = 0; h < G / 4; ++h) {  // the epilogue works on quads of states
+        const float ar4[4] = {accr[4 * h], accr[4 * h + 1], accr[4 * h + 2], accr[4 * h + 3]};
+        const float ai4[4] = {acci[4 * h], acci[4 * h + 1], acci[4 * h + 2], acci[4 * h + 3]};
+        epi.apply(r, g * (G / 4) + h, ar4, ai4);
     }
 }
 
@@ -513,12 +504,13 @@ struct EvolvePlan {
     bool tuned = false;   // cfg chosen (by the autotuner or the caller)
     bool renorm = false;  // rescale every state to norm 1 (float64) after each step
     double *part = nullptr;  // renormalisation partial sums, nrhs * kNormBlocks
-    int sp = 4;           // nrhs rounded up to a multiple of 4 (interleaved layout)
+    int sp = 4;           // interleaved layout: nrhs rounded up to a power of two >= 4 (<= 32 used)
+    int64_t n_pad = 0;    // rows rounded up to a multiple of 32
 
     bool f32() const { return mode == DIAQ_EVOLVE_MIXED || mode == DIAQ_EVOLVE_HORNER; }
     bool interleaved() const { return f32() && cfg.pipe >= 6; }
     // floats per float32 work vector (all states)
-    int64_t vlen() const { return (interleaved() ? (int64_t)sp : (int64_t)nrhs) * n; }
+    int64_t vlen() const { return interleaved() ? (int64_t)sp * n_pad : (int64_t)nrhs * n; }
 
     ~EvolvePlan() {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -537,13 +529,14 @@ struct diaq_evolve_s : public diaq_gb300::EvolvePlan {};
 namespace diaq_gb300 {
 
 // The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8) or 9 (8
-// states per thread; 4 when the padded state count is not a multiple of 8).
+// states per thread; 4 when the padded state count is 4).
 template <class Epi>
 int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &e) {
     const int v = P.cfg.pipe;
     const bool eight = v == 9 && P.sp % 8 == 0;
-    const int64_t rows_per_block = kSpmvThreads / (P.sp / (eight ? 8 : 4));
-    const unsigned g = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
+    const int groups = P.sp / (eight ? 8 : 4);          // warps per row block of 32: 1, 2, 4 or 8
+    const int64_t rows_per_block = 32 * (8 / groups);
+    const unsigned g = (unsigned)((P.n_pad + rows_per_block - 1) / rows_per_block);
     const float *are = (const float *)P.Hc->re, *aim = (const float *)P.Hc->im;
     const DiagMeta *md = P.Hc->d_meta;
     const int nd = P.Hc->nd;
@@ -570,13 +563,16 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     P->mode = mode;
     P->nrhs = nrhs;
     P->n = H.rows;
-    P->sp = (nrhs + 3) / 4 * 4;
+    P->sp = 4;
+    while (P->sp < nrhs) P->sp *= 2;
+    P->n_pad = (P->n + 31) / 32 * 32;
     int st = DIAQ_OK;
     cudaError_t e = cudaStreamCreateWithFlags(&P->s, cudaStreamNonBlocking);
     const size_t vec = (size_t)nrhs * (size_t)P->n;
     // the mixed mode sizes its 8 float vectors for the interleaved layout (>= nrhs states)
     const size_t bytes = mode == DIAQ_EVOLVE_C128 ? 6 * vec * sizeof(double)
-                                                  : 8 * (size_t)P->sp * (size_t)P->n * sizeof(float);
+                                                  : 8 * std::max<size_t>((size_t)P->sp * (size_t)P->n_pad,
+                                                                         vec) * sizeof(float);
     if (e == cudaSuccess && bytes) e = cudaMalloc(&P->buf, bytes);
     if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
     if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
@@ -743,9 +739,9 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
 static int fp32_state(EvolvePlan &P, const double *pr, const double *pi, cudaStream_t s) {
     float *var = (float *)P.buf, *vai = var + P.vlen();
     if (P.interleaved()) {
-        const int64_t cnt = P.n * P.sp;
+        const int64_t cnt = P.n_pad * P.sp;
         const int grid = (int)std::min<int64_t>((cnt + 255) / 256, 8 * num_sms());
-        to_f32_il_kernel<<<grid, 256, 0, s>>>(pr, pi, P.n, P.n, P.nrhs, P.sp, var, vai);
+        to_f32_il_kernel<<<grid, 256, 0, s>>>(pr, pi, P.n, P.n, P.n_pad, P.nrhs, P.sp, var, vai);
     } else {
         const int64_t cnt = P.nrhs * P.n;
         const int grid = (int)std::min<int64_t>((cnt + 255) / 256, 8 * num_sms());
@@ -841,7 +837,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     while (kcap < P.nrhs && kcap < 8) kcap *= 2;
     std::vector<SpmvCfg> c2;
     for (auto c : cand)
-        if (c.kmax <= kcap) c2.push_back(c);
+        if (c.kmax <= kcap && (c.pipe < 6 || P.nrhs <= 32)) c2.push_back(c);
     cand.swap(c2);
     const std::string key = tune_key(P, sl, m);
     auto cache = read_cache();
@@ -983,6 +979,7 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
             if (!(f32 && states_per_block == 4 && rows_per_thread == 1))
                 return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernel is the mixed mode's, 4 states and "
                                                    "1 row per thread");
+            if (E->nrhs > 32) return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernels take at most 32 states");
         } else if (pipelined && !(f32 && rows_per_thread == 4)) {
             return set_error(DIAQ_ERR_INVALID, "evolve: the pipelined kernels are the mixed mode's, with 4 rows per thread");
         }

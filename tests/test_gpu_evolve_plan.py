@@ -147,10 +147,11 @@ def test_prefetch_kernel_edges(native, n, variant):
 
 
 @pytest.mark.parametrize("variant", [6, 7, 9])
-@pytest.mark.parametrize("k,sl,m,renorm", [(5, 0, 11, False), (5, 1, 7, True), (8, 0, 12, False), (3, 2, 5, True)])
+@pytest.mark.parametrize("k,sl,m,renorm", [(5, 0, 11, False), (5, 1, 7, True), (8, 0, 12, False), (3, 2, 5, True),
+                                            (12, 0, 9, False), (20, 1, 6, True)])
 def test_interleaved_states(native, k, sl, m, renorm, variant):
-    """Kernel variant 6 (states interleaved per row, padded to a multiple of 4): odd and even
-    launch counts, sub-steps, renormalisation, padding states."""
+    """The interleaved kernels (states in tiles of 32 rows x 4, padded to a power of two): odd and
+    even launch counts, sub-steps, renormalisation, padding states, 1 to 8 warps per row block."""
     capi, _ = native
     A, E, P, pr, pi = _setup(capi, 11, k, capi.EVOLVE_MIXED)
     E.set_config(4, 1, variant)
