@@ -36,7 +36,7 @@ METRIC = "expm(-iHt)·ψ states·steps/s"
 # from ncu captures (profiles/), keyed by (qubits, states, form, states per block, rows per thread,
 # variant)
 TRAFFIC_PER_LAUNCH = {(20, 8, "mixed", 2, 4, 0): 809.8e6, (20, 8, "horner", 4, 1, 6): 571.6e6,
-                      (20, 8, "horner", 4, 1, 9): 555.1e6}
+                      (20, 8, "horner", 4, 1, 9): 565.6e6}
 
 
 def peaks():
