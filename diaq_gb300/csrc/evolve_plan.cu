@@ -405,9 +405,9 @@ struct EpiHornerIL {
 // one matrix load per row and diagonal, two window vectors per plane.  (Several rows per thread,
 // for a wider tile, measured slower: 2.86-3.89 ms per step against 2.53 on the 20-qubit chain.)
 //
-// U = 2 (with D = 0): two diagonals per iteration, both diagonals' matrix and window loads issued
-// before their FMAs, so each warp has two diagonals' reads in flight.
-template <class Epi, int D, int G = 4, int U = 1>
+// (Two diagonals per iteration, every load of both issued before their FMAs, measured 2.34 against
+// 2.29 ms per Horner step: 64 registers, 4 blocks per SM, no gain.)
+template <class Epi, int D, int G = 4>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_il_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                        const float *__restrict__ aim, int64_t rows, const float *__restrict__ xr,
@@ -444,42 +444,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
         for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
         __syncthreads();
         if (r >= rows) continue;
-        if constexpr (D == 0 && U == 2) {
-            int k = 0;
-            for (; k + 1 < cn; k += 2) {
-                float a[2], b[2];
-                float4 x[2][G / 4], y[2][G / 4];
-#pragma unroll
-                for (int u = 0; u < 2; ++u) {  // every load of both diagonals first
-                    const DiagMeta &m = sm[k + u];
-                    const bool in = r >= m.lo && r < m.hi;
-                    a[u] = in ? __ldcs(are + m.base + r) : 0.f;
-                    b[u] = in ? __ldcs(aim + m.base + r) : 0.f;
-#pragma unroll
-                    for (int h = 0; h < G / 4; ++h) {
-                        const int64_t at = il_at(r + m.off, g * (G / 4) + h, quads);
-                        x[u][h] = in ? __ldg(reinterpret_cast<const float4 *>(xr + at)) : make_float4(0.f, 0.f, 0.f, 0.f);
-                        y[u][h] = in ? __ldg(reinterpret_cast<const float4 *>(xi + at)) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 2; ++u)
-#pragma unroll
-                    for (int h = 0; h < G / 4; ++h) {
-                        const float xv[4] = {x[u][h].x, x[u][h].y, x[u][h].z, x[u][h].w};
-                        const float yv[4] = {y[u][h].x, y[u][h].y, y[u][h].z, y[u][h].w};
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            accr[4 * h + q] = fmaf(a[u], xv[q], accr[4 * h + q]);
-                            accr[4 * h + q] = fmaf(-b[u], yv[q], accr[4 * h + q]);
-                            acci[4 * h + q] = fmaf(a[u], yv[q], acci[4 * h + q]);
-                            acci[4 * h + q] = fmaf(b[u], xv[q], acci[4 * h + q]);
-                        }
-                    }
-            }
-            if (k < cn && r >= sm[k].lo && r < sm[k].hi)
-                term(sm[k], __ldcs(are + sm[k].base + r), __ldcs(aim + sm[k].base + r));
-        } else if constexpr (D == 0) {
+        if constexpr (D == 0) {
 #pragma unroll 4
             for (int k = 0; k < cn; ++k) {
                 if (r < sm[k].lo || r >= sm[k].hi) continue;
@@ -566,22 +531,19 @@ struct diaq_evolve_s : public diaq_gb300::EvolvePlan {};
 
 namespace diaq_gb300 {
 
-// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8), 9 (8
-// states per thread; 4 when the padded state count is 4) or 10 (as 9, two diagonals per
-// iteration).
+// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8) or 9 (8
+// states per thread; 4 when the padded state count is 4).
 template <class Epi>
 int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &e) {
     const int v = P.cfg.pipe;
-    const bool eight = (v == 9 || v == 10) && P.sp % 8 == 0;
+    const bool eight = v == 9 && P.sp % 8 == 0;
     const int groups = P.sp / (eight ? 8 : 4);          // warps per row block of 32: 1, 2, 4 or 8
     const int64_t rows_per_block = 32 * (8 / groups);
     const unsigned g = (unsigned)((P.n_pad + rows_per_block - 1) / rows_per_block);
     const float *are = (const float *)P.Hc->re, *aim = (const float *)P.Hc->im;
     const DiagMeta *md = P.Hc->d_meta;
     const int nd = P.Hc->nd;
-    if (eight && v == 10)
-        dia_spmv_il_kernel<Epi, 0, 8, 2><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
-    else if (eight)
+    if (eight)
         dia_spmv_il_kernel<Epi, 0, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
     else if (v == 7)
         dia_spmv_il_kernel<Epi, 4><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
@@ -870,7 +832,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
                 {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
                 {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
-                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}, {4, 1, 10}};
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}};
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -1013,9 +975,9 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_block < 1 || states_per_block > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_block in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
-        if (pipelined < 0 || pipelined > 10 || pipelined == 5)
+        if (pipelined < 0 || pipelined > 9 || pipelined == 5)
             return set_error(DIAQ_ERR_INVALID, "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), "
-                                               "4 (shuffled windows), 6-10 (interleaved states)");
+                                               "4 (shuffled windows), 6-9 (interleaved states)");
         if (pipelined >= 6) {
             if (!(f32 && states_per_block == 4 && rows_per_thread == 1))
                 return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernel is the mixed mode's, 4 states and "

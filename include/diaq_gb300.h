@@ -257,7 +257,7 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
  * windows as aligned vectors shifted across lanes and prefetch the matrix into L2 4 / 8 / 0
  * diagonals ahead; for the float32 modes with (4 states, 1 row), 6 / 7 / 8 keep the work vectors
  * interleaved per row (any window one aligned vector) and load the matrix 0 / 4 / 8 diagonals
- * ahead into registers, 9 with 8 states per thread, 10 as 9 with two diagonals per iteration.
+ * ahead into registers, 9 with 8 states per thread.
  * 0 states = choose automatically: on the first run the autotuner times the candidate shapes on
  * two steps of scratch copies of the states and keeps the fastest, caching the choice in a JSON
  * file (DIAQ_AUTOTUNE_CACHE, else $HOME/.cache/diaq_gb300/autotune.json).  Setting a shape drops

@@ -105,7 +105,7 @@ def test_plan_rejects_bad_input(native):
 @pytest.mark.parametrize("cfg", [(8, 1, 0), (8, 2, 0), (8, 4, 0), (4, 2, 0), (4, 4, 0), (2, 4, 0), (1, 4, 0),
                                  (1, 1, 0), (8, 4, 1), (4, 4, 1), (2, 4, 1), (1, 4, 1),
                                  (8, 4, 2), (4, 4, 2), (2, 4, 2), (1, 4, 2), (8, 4, 3), (4, 4, 3), (8, 4, 4),
-                                 (2, 4, 4), (4, 1, 6), (4, 1, 7), (4, 1, 8), (4, 1, 9), (4, 1, 10)])
+                                 (2, 4, 4), (4, 1, 6), (4, 1, 7), (4, 1, 8), (4, 1, 9)])
 def test_mixed_every_launch_shape(native, cfg):
     """Each (states per launch, rows per thread, pipelined) shape the autotuner may pick gives
     the same answer (3 states: the last launch of a chunked shape runs with masked slots)."""
@@ -146,7 +146,7 @@ def test_prefetch_kernel_edges(native, n, variant):
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
 
 
-@pytest.mark.parametrize("variant", [6, 7, 9, 10])
+@pytest.mark.parametrize("variant", [6, 7, 9])
 @pytest.mark.parametrize("k,sl,m,renorm", [(5, 0, 11, False), (5, 1, 7, True), (8, 0, 12, False), (3, 2, 5, True),
                                             (12, 0, 9, False), (20, 1, 6, True)])
 def test_interleaved_states(native, k, sl, m, renorm, variant):
@@ -169,8 +169,7 @@ def test_interleaved_states(native, k, sl, m, renorm, variant):
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, q
 
 
-@pytest.mark.parametrize("cfg", [(8, 4, 0), (2, 4, 0), (4, 2, 0), (8, 1, 0), (4, 1, 6), (4, 1, 8), (4, 1, 9),
-                                 (4, 1, 10)])
+@pytest.mark.parametrize("cfg", [(8, 4, 0), (2, 4, 0), (4, 2, 0), (8, 1, 0), (4, 1, 6), (4, 1, 8), (4, 1, 9)])
 @pytest.mark.parametrize("sl,m", [(0, 12), (1, 7), (0, 1)])
 def test_horner_accuracy(native, cfg, sl, m):
     """Horner-form float32 evaluation: within 1e-6 of the FP64 oracle after 20 steps, every
