@@ -301,6 +301,185 @@ def run_spmv_only(args):
     print(json.dumps({"mode": "spmv", "n_qubits": args.n, **out}), flush=True)
 
 
+def _spgemm_counts(n_rows, offA, offB):
+    """Result offsets and the complex multiply-adds of A B for square n_rows matrices: pair
+    (da, db) contributes one per row r with r in A's diagonal da and r + da in B's diagonal db."""
+    res, macs = set(), 0
+    for da in offA:
+        lo1, hi1 = max(0, -da), min(n_rows, n_rows - da)
+        for db in offB:
+            dc = da + db
+            if dc <= -n_rows or dc >= n_rows:
+                continue
+            lo2, hi2 = max(0, -db) - da, min(n_rows, n_rows - db) - da
+            macs += max(0, min(hi1, hi2) - max(lo1, lo2))
+            res.add(dc)
+    return sorted(res), macs
+
+
+def run_ops(args):
+    """The path's other operations on the named workloads, on the GPU, beside the CPU reference
+    (the reference's own CPU library where it was built on this host, else its C restatement):
+    12-qubit TFIM (config 1): H psi, H H (exact-zero diagonals pruned, as the CPU path does) and
+    expm_negative(H, 0.1) psi; 20-qubit XXZ (config 2): the structural dry-run and the numeric
+    SpGEMM of H H.  GPU times by CUDA events / wall clock around synchronous calls."""
+    import torch
+
+    from diaq_gb300 import build, capi
+    from diaq_gb300 import hamiltonians as ham
+    from oracle import oracle as orc
+    from oracle import reference as ref
+
+    build.build()
+    L = capi.lib()
+    peak, peak_kind = peaks()
+    dfma_peak = 0.594e12   # FP64 FMA/s measured on the pool's GB300s (throughput probe)
+    use_ref = False
+    try:
+        use_ref = ref.available() and ref.lib() is not None
+    except OSError:
+        use_ref = False
+    cpu = ref if use_ref else orc
+    kind = "reference" if use_ref else "port"
+    out = {"mode": "ops", "cpu_kind": kind, "cpu_threads": (ref.lib().ref_threads() if use_ref else orc.threads())}
+
+    def gpu_wall(fn, reps=1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    def cpu_wall(fn, reps=1):
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = fn()
+        return (time.perf_counter() - t0) / reps, r
+
+    # ---- config 1: 12-qubit TFIM ----
+    if args.ops == "xxz":
+        return _ops_xxz(args, out, L, peak, peak_kind, dfma_peak, cpu, gpu_wall, cpu_wall)
+    N, off, re, im = ham.tfim(12)
+    H = capi.Matrix.create(N, N, off, re, im)
+    Ho = orc.OMatrix(N, N, off, re, im)
+    psi = ham.random_state(N, 0)
+    xr = torch.from_numpy(psi.real.copy()).cuda()
+    xi = torch.from_numpy(psi.imag.copy()).cuda()
+    yr, yi = torch.empty_like(xr), torch.empty_like(xi)
+    sp = torch.cuda.current_stream().cuda_stream
+    spmv = lambda: capi.check(L.diaq_spmv_z(H.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), sp))
+    spmv()
+    t_spmv = gpu_wall(spmv, 200)
+
+    def product():
+        C = ctypes.c_void_p()
+        capi.check(L.diaq_spgemm(H.h, H.h, 1, None, ctypes.byref(C)))
+        capi.check(L.diaq_matrix_destroy(C))
+
+    product()
+    t_prod = gpu_wall(product, 20)
+
+    def expm():
+        U = ctypes.c_void_p()
+        s_o, m_o = ctypes.c_int(), ctypes.c_int()
+        capi.check(L.diaq_expm_negative(H.h, 0.1, 100, 1.0, 1e-12, 1, None, ctypes.byref(U), ctypes.byref(s_o),
+                                        ctypes.byref(m_o)))
+        return capi.Matrix(U)
+
+    expm()
+    t0 = time.perf_counter()
+    U = expm()
+    torch.cuda.synchronize()
+    t_expm = time.perf_counter() - t0
+    nd_U = U.info()[2]
+    del U
+    c_spmv, _ = cpu_wall(lambda: cpu.spmv(Ho, psi), 20)
+    c_prod, _ = cpu_wall(lambda: cpu.product(Ho, Ho), 3)
+    # the CPU exponential at 12 qubits fills to 8191 diagonals and takes minutes: time both at 10
+    N10, off10, re10, im10 = ham.tfim(10)
+    H10 = capi.Matrix.create(N10, N10, off10, re10, im10)
+    H10o = orc.OMatrix(N10, N10, off10, re10, im10)
+
+    def expm10():
+        U = ctypes.c_void_p()
+        s_o, m_o = ctypes.c_int(), ctypes.c_int()
+        capi.check(L.diaq_expm_negative(H10.h, 0.1, 100, 1.0, 1e-12, 1, None, ctypes.byref(U), ctypes.byref(s_o),
+                                        ctypes.byref(m_o)))
+        return capi.Matrix(U)
+
+    expm10()
+    t0 = time.perf_counter()
+    U10 = expm10()
+    torch.cuda.synchronize()
+    t_expm10 = time.perf_counter() - t0
+    c_expm10, U10c = cpu_wall(lambda: cpu.expm_negative(H10o, 0.1))
+    o10, r10, i10 = U10.download()
+    gd = orc.OMatrix(N10, N10, o10, r10, i10).to_dense()
+    cd = U10c.to_dense()
+    out["tfim12"] = {
+        "spmv": {"gpu_us": 1e6 * t_spmv, "cpu_us": 1e6 * c_spmv},
+        "product_HH": {"gpu_ms": 1e3 * t_prod, "cpu_ms": 1e3 * c_prod},
+        "expm_negative_t0.1": {"gpu_ms": 1e3 * t_expm, "result_diagonals": nd_U,
+                               "note": "CPU not timed at 12 qubits (minutes); see tfim10"},
+    }
+    out["tfim10"] = {"expm_negative_t0.1": {"gpu_ms": 1e3 * t_expm10, "cpu_ms": 1e3 * c_expm10,
+                                            "max_rel_diff_gpu_vs_cpu": float(np.abs(gd - cd).max() / np.abs(cd).max())}}
+    del H, H10, U10
+    _ops_xxz(args, out, L, peak, peak_kind, dfma_peak, cpu, gpu_wall, cpu_wall)
+
+
+def _ops_xxz(args, out, L, peak, peak_kind, dfma_peak, cpu, gpu_wall, cpu_wall):
+    """Config 2's H H at args.n qubits: dry-run and numeric SpGEMM on the GPU, the CPU product."""
+    import torch
+
+    from diaq_gb300 import capi
+    from oracle import oracle as orc
+
+    # ---- config 2: 20-qubit XXZ, H H ----
+    N, off, re, im = workload(args.n)
+    H = capi.Matrix.create(N, N, off, re, im)
+    res, macs = _spgemm_counts(N, [int(d) for d in off], [int(d) for d in off])
+    offs = np.empty(len(off) * len(off), dtype=np.int32)
+    cnt = ctypes.c_int32()
+
+    def symbolic():
+        capi.check(L.diaq_spgemm_symbolic(H.h, H.h, offs.ctypes.data, ctypes.byref(cnt), None))
+
+    symbolic()
+    t_sym = gpu_wall(symbolic, 20)
+
+    def full():
+        C = ctypes.c_void_p()
+        capi.check(L.diaq_spgemm(H.h, H.h, 0, None, ctypes.byref(C)))
+        return capi.Matrix(C)
+
+    C = full()
+    sum_c = C.info()[3]
+    del C
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    C = full()
+    torch.cuda.synchronize()
+    t_full = time.perf_counter() - t0
+    del C
+    torch.cuda.empty_cache()
+    algo_bytes = 16 * (2 * int(re.size) + sum_c) + 4 * len(off) * len(off)
+    Ho = orc.OMatrix(N, N, off, re, im)
+    c_prod20, _ = cpu_wall(lambda: cpu.product(Ho, Ho))
+    out[f"xxz{args.n}"] = {
+        "product_HH": {"gpu_ms": 1e3 * t_full, "symbolic_ms": 1e3 * t_sym, "cpu_ms": 1e3 * c_prod20,
+                       "result_offsets": int(cnt.value), "result_stored_values": int(sum_c),
+                       "complex_macs": int(macs), "algorithmic_bytes": int(algo_bytes),
+                       "gbs": algo_bytes / t_full / 1e9, "frac_hbm": algo_bytes / t_full / 1e9 / peak,
+                       "dfma_per_s": 4 * macs / t_full, "frac_fp64": 4 * macs / t_full / dfma_peak,
+                       "note": "includes the device allocation of C and the dry-run; c128 numeric is "
+                               "bound by FP64 issue (4 DFMA per complex multiply-add)"}}
+    out["peak_hbm_gbs"] = peak
+    out["peak_kind"] = peak_kind
+    print(json.dumps(out), flush=True)
+
+
 def chosen_schedule(capi, H, norm1):
     """(s, m, how) of the chosen form: the trained network's checked proposal when the package
     ships one, else the cheapest (s, m) under the remainder bound."""
@@ -734,11 +913,12 @@ def main():
     ap.add_argument("--batch-steps-c128", type=int, default=3)
     ap.add_argument("--variant", choices=["c64", "c128", "both"], default="both")
     ap.add_argument("--mem-gb", type=float, default=200.0, help="batched mode: device memory per group")
-    ap.add_argument("--mode", choices=["evolve", "spmv", "chosen", "batched", "precision"], default="evolve",
+    ap.add_argument("--mode", choices=["evolve", "spmv", "chosen", "batched", "precision", "ops"], default="evolve",
                     help="evolve: the full measurement; spmv: the SpMV kernel alone; chosen: only the chosen "
                          "form's evolution (for profiling)")
     ap.add_argument("--ref-steps", type=int, default=10, help="time steps the CPU reference arm times at most")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--ops", choices=["all", "xxz"], default="all", help="ops mode: all operations, or the XXZ H H only")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         ap.error("--warmup must be at least 3")
@@ -749,6 +929,9 @@ def main():
         return
     if args.mode == "spmv":
         run_spmv_only(args)
+        return
+    if args.mode == "ops":
+        run_ops(args)
         return
     if args.mode == "chosen":
         run_chosen_only(args)
