@@ -152,80 +152,99 @@ int spgemm_symbolic(const Matrix &A, const Matrix &B, std::vector<int32_t> &offC
 }
 
 // ---- numeric pass -------------------------------------------------------------------------------
+// Pair lists first: for every C diagonal c, the (A slot, B slot) pairs with dA + dB = dC whose
+// rows can overlap C's, in A-slot order (the reference's summation order, src/spGEMM.cpp:346-378).
+// One thread per C diagonal counts them, the host scans the counts, the same thread writes them.
+// The numeric kernel then walks only the pairs of its C diagonal -- an earlier version scanned
+// every A diagonal for every C diagonal and row tile (41 candidates for ~2.3 pairs on the
+// 20-qubit XXZ H H) and spent half its instructions on that.
+
+__device__ __forceinline__ bool pair_rows(const DiagMeta &ma, const DiagMeta &mb, const DiagMeta &mc, int64_t &lo,
+                                          int64_t &hi) {
+    // rows r with A valid (ma.lo <= r < ma.hi), B valid (mb.lo <= r + dA < mb.hi), C valid
+    lo = max(max(ma.lo, mb.lo - (int64_t)ma.off), mc.lo);
+    hi = min(min(ma.hi, mb.hi - (int64_t)ma.off), mc.hi);
+    return lo < hi;
+}
+
+// fill == nullptr: count the pairs of each C diagonal into cnt; else write them at start[c].
+__global__ void spgemm_pairs_kernel(const DiagMeta *__restrict__ mA, int ndA, const DiagMeta *__restrict__ mB,
+                                    const int32_t *__restrict__ bslot, int64_t bmin, int64_t bmax,
+                                    const DiagMeta *__restrict__ mC, int ndC, int32_t *__restrict__ cnt,
+                                    const int64_t *__restrict__ start, int2 *__restrict__ fill) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ndC; c += gridDim.x * blockDim.x) {
+        const DiagMeta mc = mC[c];
+        int64_t w = fill ? start[c] : 0;
+        int32_t n = 0;
+        for (int a = 0; a < ndA; ++a) {
+            const DiagMeta ma = mA[a];
+            const int64_t db = (int64_t)mc.off - ma.off;
+            if (db < bmin || db > bmax) continue;
+            const int32_t b = bslot[db - bmin];
+            if (b < 0) continue;
+            int64_t lo, hi;
+            if (!pair_rows(ma, mB[b], mc, lo, hi)) continue;
+            if (fill) fill[w++] = make_int2(a, b);
+            ++n;
+        }
+        if (!fill) cnt[c] = n;
+    }
+}
+
+// Block (x, y): row tile x of the C diagonals y, y + gridDim.y, ...; thread t owns V rows.
 template <typename T>
 __global__ void __launch_bounds__(kSpmvThreads)
-    spgemm_numeric_kernel(const DiagMeta *__restrict__ mA, int ndA, const T *__restrict__ Are,
-                          const T *__restrict__ Aim, const DiagMeta *__restrict__ mB,
-                          const int32_t *__restrict__ bslot, int64_t bmin, int64_t bmax,
-                          const T *__restrict__ Bre, const T *__restrict__ Bim,
-                          const DiagMeta *__restrict__ mC, int ndC, T *__restrict__ Cre,
-                          T *__restrict__ Cim) {
+    spgemm_numeric_kernel(const DiagMeta *__restrict__ mA, const T *__restrict__ Are, const T *__restrict__ Aim,
+                          const DiagMeta *__restrict__ mB, const T *__restrict__ Bre, const T *__restrict__ Bim,
+                          const DiagMeta *__restrict__ mC, int ndC, const int64_t *__restrict__ pstart,
+                          const int2 *__restrict__ pairs, T *__restrict__ Cre, T *__restrict__ Cim) {
     constexpr int V = VecOf<T>::V;
-    __shared__ DiagMeta sa[kMetaChunk];
+    const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
     for (int c = blockIdx.y; c < ndC; c += gridDim.y) {
         const DiagMeta mc = mC[c];
-        const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
-        const bool active = (r0 < mc.hi) && (r0 + V > mc.lo);
+        if (r0 >= mc.hi || r0 + V <= mc.lo) continue;
         T accr[V], acci[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) accr[v] = acci[v] = (T)0;
-        // whole block leaves together when its tile misses this diagonal
-        const int64_t tile0 = (int64_t)blockIdx.x * kSpmvThreads * V;
-        const bool tile_hit = (tile0 < mc.hi) && (tile0 + (int64_t)kSpmvThreads * V > mc.lo);
-        if (!tile_hit) continue;
-        for (int a0 = 0; a0 < ndA; a0 += kMetaChunk) {
-            const int an = min(kMetaChunk, ndA - a0);
-            __syncthreads();
-            for (int i = threadIdx.x; i < an; i += kSpmvThreads) sa[i] = mA[a0 + i];
-            __syncthreads();
-            if (!active) continue;
-            for (int a = 0; a < an; ++a) {
-                const DiagMeta ma = sa[a];
-                const int64_t db = (int64_t)mc.off - ma.off;
-                if (db < bmin || db > bmax) continue;
-                const int32_t b = bslot[db - bmin];
-                if (b < 0) continue;
-                const DiagMeta mb = mB[b];
-                // rows r with A valid (ma.lo <= r < ma.hi), B valid (mb.lo <= r + dA < mb.hi),
-                // C valid (mc.lo <= r < mc.hi)
-                const int64_t lo = max(max(ma.lo, mb.lo - (int64_t)ma.off), mc.lo);
-                const int64_t hi = min(min(ma.hi, mb.hi - (int64_t)ma.off), mc.hi);
-                if (r0 + V <= lo || r0 >= hi) continue;
-                T ar[V], ai[V], br[V], bi[V];
-                load_vec<T, V>(ar, Are + ma.base + r0);
-                load_vec<T, V>(ai, Aim + ma.base + r0);
-                const bool full = (r0 >= lo) && (r0 + V <= hi);
-                const T *pbr = Bre + mb.base + r0 + ma.off;
-                const T *pbi = Bim + mb.base + r0 + ma.off;
-                if (full && aligned16(pbr)) {
-                    load_vec<T, V>(br, pbr);
-                    load_vec<T, V>(bi, pbi);
-                } else {
-#pragma unroll
-                    for (int v = 0; v < V; ++v) {
-                        const bool ok = (r0 + v >= lo) && (r0 + v < hi);
-                        br[v] = ok ? __ldg(pbr + v) : (T)0;
-                        bi[v] = ok ? __ldg(pbi + v) : (T)0;
-                        if (!ok) ar[v] = ai[v] = (T)0;
-                    }
-                }
+        const int64_t p1 = pstart[c + 1];
+        for (int64_t p = pstart[c]; p < p1; ++p) {
+            const int2 ab = pairs[p];
+            const DiagMeta ma = mA[ab.x], mb = mB[ab.y];
+            int64_t lo, hi;
+            pair_rows(ma, mb, mc, lo, hi);
+            if (r0 + V <= lo || r0 >= hi) continue;
+            T ar[V], ai[V], br[V], bi[V];
+            load_vec<T, V>(ar, Are + ma.base + r0);
+            load_vec<T, V>(ai, Aim + ma.base + r0);
+            const bool full = (r0 >= lo) && (r0 + V <= hi);
+            const T *pbr = Bre + mb.base + r0 + ma.off;
+            const T *pbi = Bim + mb.base + r0 + ma.off;
+            if (full && aligned16(pbr)) {
+                load_vec<T, V>(br, pbr);
+                load_vec<T, V>(bi, pbi);
+            } else {
 #pragma unroll
                 for (int v = 0; v < V; ++v) {
-                    accr[v] = fma(ar[v], br[v], accr[v]);
-                    accr[v] = fma(-ai[v], bi[v], accr[v]);
-                    acci[v] = fma(ar[v], bi[v], acci[v]);
-                    acci[v] = fma(ai[v], br[v], acci[v]);
+                    const bool ok = (r0 + v >= lo) && (r0 + v < hi);
+                    br[v] = ok ? __ldg(pbr + v) : (T)0;
+                    bi[v] = ok ? __ldg(pbi + v) : (T)0;
+                    if (!ok) ar[v] = ai[v] = (T)0;
                 }
             }
-        }
-        if (active) {
 #pragma unroll
             for (int v = 0; v < V; ++v) {
-                const int64_t r = r0 + v;
-                if (r >= mc.lo && r < mc.hi) {
-                    Cre[mc.base + r] = accr[v];
-                    Cim[mc.base + r] = acci[v];
-                }
+                accr[v] = fma(ar[v], br[v], accr[v]);
+                accr[v] = fma(-ai[v], bi[v], accr[v]);
+                acci[v] = fma(ar[v], bi[v], acci[v]);
+                acci[v] = fma(ai[v], br[v], acci[v]);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int64_t r = r0 + v;
+            if (r >= mc.lo && r < mc.hi) {
+                Cre[mc.base + r] = accr[v];
+                Cim[mc.base + r] = acci[v];
             }
         }
     }
@@ -243,27 +262,55 @@ int spgemm_numeric(const Matrix &A, const Matrix &B, Matrix &C, cudaStream_t s) 
     const int64_t span = bmax - bmin + 1;
     std::vector<int32_t> map((size_t)span, -1);
     for (int32_t k = 0; k < B.nd; ++k) map[(size_t)(B.off[k] - bmin)] = k;
-    int32_t *dmap = nullptr;
-    DQ_CUDA(cudaMallocAsync(&dmap, sizeof(int32_t) * span, s));
-    cudaError_t e = cudaMemcpyAsync(dmap, map.data(), sizeof(int32_t) * span, cudaMemcpyHostToDevice, s);
+    // scratch: B map, per-C counts, per-C starts
+    const size_t mbytes = sizeof(int32_t) * (size_t)span, cbytes = sizeof(int32_t) * (size_t)C.nd,
+                 sbytes = sizeof(int64_t) * ((size_t)C.nd + 1);
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    uint8_t *scratch = nullptr;
+    DQ_CUDA(cudaMallocAsync(&scratch, up(mbytes) + up(cbytes) + sbytes, s));
+    int32_t *dmap = (int32_t *)scratch;
+    int32_t *dcnt = (int32_t *)(scratch + up(mbytes));
+    int64_t *dstart = (int64_t *)(scratch + up(mbytes) + up(cbytes));
+    int2 *dpairs = nullptr;
+    std::vector<int32_t> cnt((size_t)C.nd);
+    std::vector<int64_t> start((size_t)C.nd + 1, 0);
+    const int pg = (int)std::max<int64_t>(1, std::min<int64_t>((C.nd + 127) / 128, 4 * num_sms()));
+    cudaError_t e = cudaMemcpyAsync(dmap, map.data(), mbytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
+        spgemm_pairs_kernel<<<pg, 128, 0, s>>>(A.d_meta, A.nd, B.d_meta, dmap, bmin, bmax, C.d_meta, C.nd, dcnt,
+                                               nullptr, nullptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cnt.data(), dcnt, cbytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) {
+        for (int32_t c = 0; c < C.nd; ++c) start[(size_t)c + 1] = start[(size_t)c] + cnt[(size_t)c];
+        const int64_t npairs = start[(size_t)C.nd];
+        e = cudaMemcpyAsync(dstart, start.data(), sbytes, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMallocAsync((void **)&dpairs, sizeof(int2) * (size_t)std::max<int64_t>(npairs, 1), s);
+    }
+    if (e == cudaSuccess) {
+        spgemm_pairs_kernel<<<pg, 128, 0, s>>>(A.d_meta, A.nd, B.d_meta, dmap, bmin, bmax, C.d_meta, C.nd, nullptr,
+                                               dstart, dpairs);
         int64_t maxrows = 1;
         for (const auto &m : C.meta) maxrows = std::max(maxrows, m.hi);
         const int V = A.prec == DIAQ_C128 ? 2 : 4;
-        const dim3 grid(spmv_blocks(maxrows, V), (unsigned)std::min<int64_t>(C.nd, 65535));
+        // up to 64 C diagonals per block row: each block walks several diagonals' pairs
+        const dim3 grid(spmv_blocks(maxrows, V), (unsigned)std::min<int64_t>(C.nd, 64));
         if (A.prec == DIAQ_C128)
             spgemm_numeric_kernel<double><<<grid, kSpmvThreads, 0, s>>>(
-                A.d_meta, A.nd, (const double *)A.re, (const double *)A.im, B.d_meta, dmap, bmin, bmax,
-                (const double *)B.re, (const double *)B.im, C.d_meta, C.nd, (double *)C.re, (double *)C.im);
+                A.d_meta, (const double *)A.re, (const double *)A.im, B.d_meta, (const double *)B.re,
+                (const double *)B.im, C.d_meta, C.nd, dstart, dpairs, (double *)C.re, (double *)C.im);
         else
             spgemm_numeric_kernel<float><<<grid, kSpmvThreads, 0, s>>>(
-                A.d_meta, A.nd, (const float *)A.re, (const float *)A.im, B.d_meta, dmap, bmin, bmax,
-                (const float *)B.re, (const float *)B.im, C.d_meta, C.nd, (float *)C.re, (float *)C.im);
+                A.d_meta, (const float *)A.re, (const float *)A.im, B.d_meta, (const float *)B.re,
+                (const float *)B.im, C.d_meta, C.nd, dstart, dpairs, (float *)C.re, (float *)C.im);
         e = cudaGetLastError();
     }
-    // the host map must outlive the async copy
+    // the host vectors must outlive the async copies
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFreeAsync(dmap, s);
+    if (dpairs) cudaFreeAsync(dpairs, s);
+    cudaFreeAsync(scratch, s);
     if (e != cudaSuccess) return cuda_status(e, "spgemm numeric", __FILE__, __LINE__);
     return DIAQ_OK;
 }
