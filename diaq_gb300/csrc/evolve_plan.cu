@@ -22,6 +22,7 @@
 //   MIXED: psi (caller's, float64); v_a, v_b, hi, lo           (float32)
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -845,7 +846,11 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     const std::string key = tune_key(P, sl, m);
     auto cache = read_cache();
     auto hit = cache.find(key);
-    if (hit != cache.end()) {
+    // a cached shape is used only if it is still one of this build's candidates
+    const bool known = hit != cache.end() && std::any_of(cand.begin(), cand.end(), [&](const SpmvCfg &c) {
+                           return c.kmax == hit->second.kmax && c.vr == hit->second.vr && c.pipe == hit->second.pipe;
+                       });
+    if (known) {
         P.cfg = hit->second;
         P.tuned = true;
         return DIAQ_OK;
