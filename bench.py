@@ -575,7 +575,8 @@ def run_batched(args):
     mine = partition_instances([k * (2 * n + 1) * (1 << n) for _, n, k, _ in specs], world)[rank]
     specs = [specs[i] for i in mine]
     dt, tol = 0.02, TOL_STEP
-    out = {"mode": "batched", "horner": args.horner, "instances": args.instances, "n_range": [args.n_lo, args.n_hi], "dt": dt,
+    out = {"mode": "batched", "horner": args.horner, "interleaved": not args.planar, "instances": args.instances,
+           "n_range": [args.n_lo, args.n_hi], "dt": dt,
            "states": all_states, "n_gpus": world, "scaling": "weak" if world > 1 else None, "variants": {}}
     for variant in (["c64", "c128"] if args.variant == "both" else [args.variant]):
         prec = capi.C64 if variant == "c64" else capi.C128
@@ -613,6 +614,7 @@ def run_batched(args):
             start = {j: (prs[j][0].cpu().numpy() + 1j * pis[j][0].cpu().numpy()) for j in small}
             B = capi.Batch(mats, prs, pis)
             B.set_horner(args.horner)
+            B.set_interleaved(not args.planar)
             if variant == "c128":
                 B.set_config(4, 2)   # FP64-bound either way; autotuning would cost minutes of steps
             stream = torch.cuda.current_stream()
@@ -913,6 +915,8 @@ def main():
     ap.add_argument("--batch-steps-c128", type=int, default=3)
     ap.add_argument("--variant", choices=["c64", "c128", "both"], default="both")
     ap.add_argument("--mem-gb", type=float, default=200.0, help="batched mode: device memory per group")
+    ap.add_argument("--planar", action="store_true",
+                    help="batched mode: keep every instance's work vectors planar (no interleaved tiles)")
     ap.add_argument("--mode", choices=["evolve", "spmv", "chosen", "batched", "precision", "ops"], default="evolve",
                     help="evolve: the full measurement; spmv: the SpMV kernel alone; chosen: only the chosen "
                          "form's evolution (for profiling)")

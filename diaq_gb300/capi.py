@@ -68,6 +68,7 @@ SIGNATURES = {
     "diaq_batch_set_config": (INT, [P, INT, INT]),
     "diaq_batch_config": (INT, [P, P, P, P]),
     "diaq_batch_set_horner": (INT, [P, INT]),
+    "diaq_batch_set_interleaved": (INT, [P, INT]),
     "diaq_mlp_num_params": (INT, []),
     "diaq_mlp_create": (INT, [ctypes.c_uint64, P]),
     "diaq_mlp_destroy": (INT, [P]),
@@ -328,6 +329,9 @@ class Batch:
 
     def set_horner(self, on: bool = True):
         check(lib().diaq_batch_set_horner(self.h, 1 if on else 0))
+
+    def set_interleaved(self, on: bool = True):
+        check(lib().diaq_batch_set_interleaved(self.h, 1 if on else 0))
 
     def config(self):
         k, v, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

@@ -20,6 +20,14 @@
 // (-i tau/(k+1)) H w_{k+1}, psi += (-i tau) H w_1 in float64 -- no running sum.  T(psi) stays in
 // v_a for the whole sub-step (the last term refreshes it), w alternates between v_b and the
 // otherwise unused hi vectors, and no copy phase is needed.
+//
+// Interleaved instances.  A complex64 instance with 4 to 32 states keeps its float32 work vectors
+// in the tiled interleaved layout (spmv_il.cuh: 32 rows x 4 states per 512-byte tile, the states
+// padded to sp, a power of two) and runs in a second kernel of the same phase: one block per
+// block of rows and all sp states, G = 8 states per thread when sp is a multiple of 8, else 4.
+// Every window load of a warp is then one contiguous 512-byte run and every matrix value is read
+// once per row block for all the states.  The other instances (1-3 or more than 32 states,
+// complex128) keep the planar layout and the persistent kernel above.
 #include <sys/stat.h>
 
 #include <algorithm>
@@ -32,7 +40,7 @@
 #include <string>
 #include <vector>
 
-#include "spmv_kernel.cuh"
+#include "spmv_il.cuh"
 
 namespace diaq_gb300 {
 
@@ -44,6 +52,9 @@ struct BatchInst {
     int m, phases;   // Taylor terms per sub-step; launches per step (2^s m, +1 when odd)
     int sub;         // 2^s
     int horner;      // Horner evaluation (m >= 2 and the batch's form)
+    int il_ok, il;   // may use / uses the interleaved layout
+    int sp;          // interleaved: states padded to a power of two >= 4
+    int64_t n_pad;   // interleaved: rows padded to a multiple of 32
     double tau;      // dt / 2^s
     double *pr, *pi; // states, leading dimension rows
     void *var, *vai, *vbr, *vbi, *hr, *hi, *lr, *li;  // T work vectors, leading dimension rows
@@ -53,16 +64,15 @@ struct BatchItem {
     int inst, tile, chunk, pad;
 };
 
-__device__ __forceinline__ void two_sum_t(float a, float b, float &s, float &e) {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
+// TwoSum with unfused adds (as spmv_il.cuh's two_sum), and an unfused add, per precision.
+__device__ __forceinline__ void two_sum_t(float a, float b, float &s, float &e) { two_sum(a, b, s, e); }
 __device__ __forceinline__ void two_sum_t(double a, double b, double &s, double &e) {
-    s = a + b;
-    const double bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
+    s = __dadd_rn(a, b);
+    const double bb = __dsub_rn(s, a);
+    e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
 }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 
 // phase < 0: initialise v_a = T(psi) for every item.
 template <typename T, int K, int VR>
@@ -184,8 +194,8 @@ __global__ void __launch_bounds__(kSpmvThreads)
                     const int64_t i = (int64_t)(q0 + q) * ld + r;
                     const T tr = acci[q][v] * scale, ti = -accr[q][v] * scale;
                     if (!last) {
-                        outr[i] = fr[i] + tr;
-                        outi[i] = fi[i] + ti;
+                        outr[i] = add_rn(fr[i], tr);
+                        outi[i] = add_rn(fi[i], ti);
                     } else {  // this launch reads w_1, not T(psi): refreshing it here is safe
                         const double nr = I.pr[i] + (double)tr, ni = I.pi[i] + (double)ti;
                         I.pr[i] = nr;
@@ -241,17 +251,122 @@ __global__ void __launch_bounds__(kSpmvThreads)
     }
 }
 
+// One item of an interleaved instance: row block `tile` (32 * 8 / (sp / G) rows) and all sp
+// states.  Phases as in batched_phase_kernel; the initialisation and copy phases move the item's
+// rows of every state, which are one contiguous range of the tiled vectors.
+template <int G>
+__device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm, int64_t tile, int phase) {
+    const int quads = I.sp >> 2, groups = I.sp / G;
+    const int64_t rpb = 32 * (8 / groups);
+    const int64_t r0 = tile * rpb, ld = I.rows;
+    float *var = (float *)I.var, *vai = (float *)I.vai, *vbr = (float *)I.vbr, *vbi = (float *)I.vbi;
+    if (phase < 0 || phase >= I.sub * I.m) {
+        const bool init = phase < 0;
+        const bool copy = !init && phase == I.sub * I.m && (I.phases > I.sub * I.m);
+        if (!init && !copy) return;
+        const int64_t e1 = min(r0 + rpb, I.n_pad) * I.sp;
+        for (int64_t e = r0 * I.sp + threadIdx.x; e < e1; e += blockDim.x) {
+            if (init) {  // element e of the tiled vector is state q of row r
+                const int64_t blk = e / (quads * 128);
+                const int rem = (int)(e - blk * quads * 128);
+                const int64_t r = blk * 32 + ((rem & 127) >> 2);
+                const int q = (rem >> 7) * 4 + (rem & 3);
+                const bool live = r < I.rows && q < I.nrhs;
+                var[e] = live ? (float)I.pr[q * ld + r] : 0.f;
+                vai[e] = live ? (float)I.pi[q * ld + r] : 0.f;
+            } else {
+                var[e] = vbr[e];
+                vai[e] = vbi[e];
+            }
+        }
+        return;
+    }
+    const int k = phase % I.m + 1;
+    const bool first = (k == 1), last = (k == I.m);
+    const float *xr, *xi;
+    float *outr, *outi;
+    if (I.horner) {
+        xr = first ? var : ((k - 1) & 1) ? vbr : (float *)I.hr;
+        xi = first ? vai : ((k - 1) & 1) ? vbi : (float *)I.hi;
+        outr = (k & 1) ? vbr : (float *)I.hr;
+        outi = (k & 1) ? vbi : (float *)I.hi;
+    } else {
+        xr = (phase & 1) ? vbr : var;
+        xi = (phase & 1) ? vbi : vai;
+        outr = (phase & 1) ? var : vbr;
+        outi = (phase & 1) ? vai : vbi;
+    }
+    const int wid = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    const int g = wid % groups;
+    const int64_t r = r0 + (int64_t)(wid / groups) * 32 + lane;
+    float accr[G], acci[G];
+#pragma unroll
+    for (int q = 0; q < G; ++q) accr[q] = acci[q] = 0.f;
+    const float *are = (const float *)I.are, *aim = (const float *)I.aim;
+    for (int c0 = 0; c0 < I.nd; c0 += kMetaChunk) {
+        const int cn = min(kMetaChunk, I.nd - c0);
+        __syncthreads();
+        for (int j = threadIdx.x; j < cn; j += kSpmvThreads) sm[j] = I.meta[c0 + j];
+        __syncthreads();
+        if (r >= I.rows) continue;
+#pragma unroll 4
+        for (int j = 0; j < cn; ++j) {
+            if (r < sm[j].lo || r >= sm[j].hi) continue;
+            il_term<G>(r + sm[j].off, g * (G / 4), quads, __ldcs(are + sm[j].base + r), __ldcs(aim + sm[j].base + r), xr,
+                       xi, accr, acci);
+        }
+    }
+    if (r >= I.rows) return;
+    if (I.horner) {  // the last step reads w_1, not fp32(psi): refreshing v_a there is safe
+        const EpiHornerIL e{outr, outi, var, vai, var, vai, I.pr, I.pi, ld, I.sp, I.nrhs,
+                            (float)(I.tau / (double)(I.m - k + 1)), last};
+#pragma unroll
+        for (int h = 0; h < G / 4; ++h) {
+            const float ar4[4] = {accr[4 * h], accr[4 * h + 1], accr[4 * h + 2], accr[4 * h + 3]};
+            const float ai4[4] = {acci[4 * h], acci[4 * h + 1], acci[4 * h + 2], acci[4 * h + 3]};
+            e.apply(r, g * (G / 4) + h, ar4, ai4);
+        }
+    } else {
+        const EpiMixedIL e{outr, outi, (float *)I.hr, (float *)I.hi, (float *)I.lr, (float *)I.li, I.pr, I.pi, ld, I.sp,
+                           I.nrhs, (float)(I.tau / (double)k), first, last};
+#pragma unroll
+        for (int h = 0; h < G / 4; ++h) {
+            const float ar4[4] = {accr[4 * h], accr[4 * h + 1], accr[4 * h + 2], accr[4 * h + 3]};
+            const float ai4[4] = {acci[4 * h], acci[4 * h + 1], acci[4 * h + 2], acci[4 * h + 3]};
+            e.apply(r, g * (G / 4) + h, ar4, ai4);
+        }
+    }
+}
+
+// Items of the instances with G states per thread (separate lists and launches for G = 8 and 4,
+// so that each kernel keeps only its own registers).
+template <int G>
+__global__ void __launch_bounds__(kSpmvThreads, 4)
+    batched_il_kernel(const BatchInst *__restrict__ insts, const BatchItem *__restrict__ items, int phase) {
+    __shared__ DiagMeta sm[kMetaChunk];
+    __shared__ BatchInst si;
+    const BatchItem item = items[blockIdx.x];
+    if (threadIdx.x == 0) si = insts[item.inst];
+    __syncthreads();
+    batched_il_item<G>(si, sm, item.tile, phase);
+}
+
 struct Batch {
     int prec = DIAQ_C64;
     std::vector<BatchInst> inst;      // host copy
     std::vector<int64_t> rows;
     BatchInst *d_inst = nullptr;
-    BatchItem *d_items = nullptr;
+    BatchItem *d_items = nullptr;     // planar instances
     int n_items = 0;
+    BatchItem *d_il_items = nullptr;  // interleaved instances, one block each: G = 8 first, then G = 4
+    int n_il_items = 0, n_il8 = 0;
+    bool il_on = true;                // interleave the instances that can be
+    int items_il = -1;                // il_on of the current item lists
     void *work = nullptr;
     cudaStream_t s = nullptr;         // capture stream
     SpmvCfg cfg{8, 0};
     bool tuned = false;
+    bool user_cfg = false;            // shape set by the caller
     int items_cfg_k = 0, items_cfg_vr = 0;
     cudaGraphExec_t graph = nullptr;
     std::vector<int> graph_key;       // (s_i, m_i) of the recorded graph, plus dt bits
@@ -262,6 +377,7 @@ struct Batch {
         if (graph) cudaGraphExecDestroy(graph);
         cudaFree(d_inst);
         cudaFree(d_items);
+        cudaFree(d_il_items);
         cudaFree(work);
         if (s) cudaStreamDestroy(s);
     }
@@ -278,31 +394,47 @@ static int vr_of(const Batch &B) { return B.cfg.vr > 0 ? B.cfg.vr : (B.prec == D
 // Item list for the current launch shape: largest instances first.
 static int build_items(Batch &B) {
     const int K = B.cfg.kmax, VR = vr_of(B);
-    if (B.d_items && B.items_cfg_k == K && B.items_cfg_vr == VR) return DIAQ_OK;
+    if (B.d_items && B.items_cfg_k == K && B.items_cfg_vr == VR && B.items_il == (int)B.il_on) return DIAQ_OK;
     std::vector<int> order(B.inst.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         return B.inst[a].rows * B.inst[a].nd * B.inst[a].nrhs > B.inst[b].rows * B.inst[b].nd * B.inst[b].nrhs;
     });
-    std::vector<BatchItem> items;
+    std::vector<BatchItem> items, il_items, il4_items;
     for (int i : order) {
+        const BatchInst &I = B.inst[i];
+        if (I.il) {
+            const bool eight = I.sp % 8 == 0;
+            const int64_t rpb = 32 * (8 / (I.sp / (eight ? 8 : 4)));
+            for (int64_t t = 0; t < (I.rows + rpb - 1) / rpb; ++t)
+                (eight ? il_items : il4_items).push_back(BatchItem{i, (int)t, 0, 0});
+            continue;
+        }
         const int64_t tiles = (B.inst[i].rows + (int64_t)kSpmvThreads * VR - 1) / ((int64_t)kSpmvThreads * VR);
         const int chunks = (B.inst[i].nrhs + K - 1) / K;
         for (int64_t t = 0; t < tiles; ++t)
             for (int c = 0; c < chunks; ++c) items.push_back(BatchItem{i, (int)t, c, 0});
     }
+    B.n_il8 = (int)il_items.size();
+    il_items.insert(il_items.end(), il4_items.begin(), il4_items.end());
     if (B.d_items) cudaFree(B.d_items);
-    B.d_items = nullptr;
+    if (B.d_il_items) cudaFree(B.d_il_items);
+    B.d_items = B.d_il_items = nullptr;
     DQ_CUDA(cudaMalloc(&B.d_items, sizeof(BatchItem) * std::max<size_t>(items.size(), 1)));
+    DQ_CUDA(cudaMalloc(&B.d_il_items, sizeof(BatchItem) * std::max<size_t>(il_items.size(), 1)));
     DQ_CUDA(cudaMemcpy(B.d_items, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice));
+    DQ_CUDA(cudaMemcpy(B.d_il_items, il_items.data(), sizeof(BatchItem) * il_items.size(), cudaMemcpyHostToDevice));
     B.n_items = (int)items.size();
+    B.n_il_items = (int)il_items.size();
     B.items_cfg_k = K;
     B.items_cfg_vr = VR;
+    B.items_il = (int)B.il_on;
     return DIAQ_OK;
 }
 
 template <typename T, int K, int VR>
 static int launch_phase_t(const Batch &B, int phase, cudaStream_t s) {
+    if (B.n_items == 0) return DIAQ_OK;
     static int blocks_per_sm = 0;
     if (blocks_per_sm == 0) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, batched_phase_kernel<T, K, VR>, kSpmvThreads, 0);
@@ -336,7 +468,12 @@ static int launch_phase(const Batch &B, int phase, cudaStream_t s) {
 }
 
 static int phase(const Batch &B, int p, cudaStream_t s) {
-    return B.prec == DIAQ_C64 ? launch_phase<float>(B, p, s) : launch_phase<double>(B, p, s);
+    DQ_TRY(B.prec == DIAQ_C64 ? launch_phase<float>(B, p, s) : launch_phase<double>(B, p, s));
+    if (B.n_il8 > 0) batched_il_kernel<8><<<B.n_il8, kSpmvThreads, 0, s>>>(B.d_inst, B.d_il_items, p);
+    if (B.n_il_items > B.n_il8)
+        batched_il_kernel<4><<<B.n_il_items - B.n_il8, kSpmvThreads, 0, s>>>(B.d_inst, B.d_il_items + B.n_il8, p);
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
 }
 
 // Per-instance schedules into the device table.
@@ -350,6 +487,7 @@ static int set_schedule(Batch &B, double dt, const int *sl, const int *m) {
         I.m = m[i];
         I.tau = dt / (double)I.sub;
         I.horner = B.horner && I.m >= 2;
+        I.il = I.il_ok && B.il_on;
         const int launches = I.sub * I.m;
         I.phases = I.horner ? launches : launches + (launches & 1);
         B.max_phases = std::max(B.max_phases, I.phases);
@@ -419,9 +557,11 @@ static void cache_store(const std::string &key, int k, int v) {
 
 static std::string batch_key(const Batch &B) {
     int64_t rows = 0, states = 0;
+    int il = 0;
     for (const auto &I : B.inst) {
         rows += I.rows;
         states += I.nrhs * I.rows;
+        il += I.il;
     }
     int dev = 0;
     cudaGetDevice(&dev);
@@ -431,14 +571,18 @@ static std::string batch_key(const Batch &B) {
     for (auto &ch : name)
         if (ch == '"' || ch == ' ') ch = '_';
     char buf[256];
-    std::snprintf(buf, sizeof(buf), "%s|batch|%s%s|inst=%zu|rows=%lld|staterows=%lld|phases=%d", name.c_str(),
-                  B.prec == DIAQ_C64 ? "c64" : "c128", B.horner ? "|horner" : "", B.inst.size(), (long long)rows,
-                  (long long)states, B.max_phases);
+    std::snprintf(buf, sizeof(buf), "%s|batch|%s%s|inst=%zu|il=%d|rows=%lld|staterows=%lld|phases=%d",
+                  name.c_str(), B.prec == DIAQ_C64 ? "c64" : "c128", B.horner ? "|horner" : "", B.inst.size(), il,
+                  (long long)rows, (long long)states, B.max_phases);
     return buf;
 }
 
 // Time one step per candidate shape on scratch states (the caller's are saved and restored).
 static int autotune(Batch &B) {
+    if (std::all_of(B.inst.begin(), B.inst.end(), [](const BatchInst &I) { return I.il != 0; })) {
+        B.tuned = true;  // no planar instance: the shape is unused
+        return DIAQ_OK;
+    }
     const std::string key = batch_key(B);
     int k = 0, v = 0;
     // a cached shape is used only if this build can launch it
@@ -521,20 +665,35 @@ int diaq_batch_create(int n_inst, const diaq_matrix_t *H, const int *nrhs, doubl
                       double *const *psi_im, diaq_batch_t *out) {
     if (!out || n_inst < 1 || !H || !nrhs || !psi_re || !psi_im) return set_error(DIAQ_ERR_INVALID, "batch: bad argument");
     const int prec = H[0] ? H[0]->prec : DIAQ_C64;
-    size_t work_elems = 0;
+    const size_t esz = prec == DIAQ_C64 ? sizeof(float) : sizeof(double);
+    // one work vector of instance i: planar nrhs x rows, or tiled sp x n_pad (complex64, 4-32 states),
+    // rounded up to 256 bytes so that every vector starts aligned for 16-byte loads
+    auto il_shape = [&](int i, int &sp, int64_t &n_pad) {
+        sp = 4;
+        while (sp < nrhs[i]) sp *= 2;
+        n_pad = (H[i]->rows + 31) / 32 * 32;
+        return prec == DIAQ_C64 && nrhs[i] >= 4 && nrhs[i] <= 32;
+    };
+    auto vec_bytes = [&](int i) {
+        int sp;
+        int64_t n_pad;
+        size_t e = (size_t)nrhs[i] * (size_t)H[i]->rows;
+        if (il_shape(i, sp, n_pad)) e = std::max(e, (size_t)sp * (size_t)n_pad);
+        return (e * esz + 255) / 256 * 256;
+    };
+    size_t work_bytes = 0;
     for (int i = 0; i < n_inst; ++i) {
         if (!H[i] || !psi_re[i] || !psi_im[i]) return set_error(DIAQ_ERR_INVALID, "batch: NULL matrix or state pointer");
         if (H[i]->rows != H[i]->cols) return set_error(DIAQ_ERR_INVALID, "batch: every H must be square");
         if (H[i]->prec != prec) return set_error(DIAQ_ERR_INVALID, "batch: all matrices must have the same precision");
         if (prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "batch: c128 or c64 matrices only");
         if (nrhs[i] < 1) return set_error(DIAQ_ERR_INVALID, "batch: every instance needs at least one state");
-        work_elems += (size_t)nrhs[i] * (size_t)H[i]->rows;
+        work_bytes += 8 * vec_bytes(i);
     }
     diaq_batch_s *B = new diaq_batch_s();
     B->prec = prec;
-    const size_t esz = prec == DIAQ_C64 ? sizeof(float) : sizeof(double);
     cudaError_t e = cudaStreamCreateWithFlags(&B->s, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&B->work, 8 * work_elems * esz + 256);
+    if (e == cudaSuccess) e = cudaMalloc(&B->work, work_bytes + 256);
     if (e == cudaSuccess) e = cudaMalloc(&B->d_inst, sizeof(BatchInst) * n_inst);
     if (e != cudaSuccess) {
         delete B;
@@ -551,7 +710,8 @@ int diaq_batch_create(int n_inst, const diaq_matrix_t *H, const int *nrhs, doubl
         I.nrhs = nrhs[i];
         I.pr = psi_re[i];
         I.pi = psi_im[i];
-        const size_t vb = (size_t)nrhs[i] * (size_t)H[i]->rows * esz;
+        I.il_ok = il_shape(i, I.sp, I.n_pad) ? 1 : 0;
+        const size_t vb = vec_bytes(i);
         void **slots[8] = {&I.var, &I.vai, &I.vbr, &I.vbi, &I.hr, &I.hi, &I.lr, &I.li};
         for (int j = 0; j < 8; ++j) {
             *slots[j] = w;
@@ -571,14 +731,14 @@ int diaq_batch_destroy(diaq_batch_t B) {
 int diaq_batch_set_config(diaq_batch_t B, int states_per_launch, int rows_per_thread) {
     if (!B) return set_error(DIAQ_ERR_INVALID, "batch is NULL");
     if (states_per_launch == 0) {
-        B->tuned = false;
+        B->tuned = B->user_cfg = false;
     } else {
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (B->prec == DIAQ_C64 && rows_per_thread == 4);
         if (!(states_per_launch == 1 || states_per_launch == 2 || states_per_launch == 4 || states_per_launch == 8) ||
             !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "batch: states_per_launch 1, 2, 4 or 8; rows_per_thread 1, 2 (4 for c64)");
         B->cfg = SpmvCfg{states_per_launch, rows_per_thread};
-        B->tuned = true;
+        B->tuned = B->user_cfg = true;
     }
     if (B->graph) cudaGraphExecDestroy(B->graph);
     B->graph = nullptr;
@@ -591,6 +751,17 @@ int diaq_batch_set_horner(diaq_batch_t B, int on) {
         B->horner = on != 0;
         if (B->graph) cudaGraphExecDestroy(B->graph);
         B->graph = nullptr;  // the schedule (phases per instance) is rebuilt on the next run
+    }
+    return DIAQ_OK;
+}
+
+int diaq_batch_set_interleaved(diaq_batch_t B, int on) {
+    if (!B) return set_error(DIAQ_ERR_INVALID, "batch is NULL");
+    if (B->il_on != (on != 0)) {
+        B->il_on = on != 0;
+        if (!B->user_cfg) B->tuned = false;  // other planar instances: tune again (or use the cache)
+        if (B->graph) cudaGraphExecDestroy(B->graph);
+        B->graph = nullptr;
     }
     return DIAQ_OK;
 }

@@ -32,6 +32,7 @@
 #include <string>
 #include <tuple>
 
+#include "spmv_il.cuh"
 #include "spmv_pipe.cuh"
 
 namespace diaq_gb300 {
@@ -77,12 +78,6 @@ struct EpiPlain {
             }
     }
 };
-
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
 
 // Mixed term k of a sub-step: t = (-i*scale) * (A v) in float32;
 //   k == 1:  hi = t, lo = 0;  else (hi, e) = TwoSum(hi, t), lo += e;
@@ -187,8 +182,8 @@ struct EpiHorner {
                 const int64_t i = q * ld + r;
                 const float tr = si[q][v] * scale, ti = -sr[q][v] * scale;
                 if (!last) {
-                    wr[i] = fr[i] + tr;
-                    wi[i] = fi[i] + ti;
+                    wr[i] = __fadd_rn(fr[i], tr);  // unfused, as the interleaved epilogue
+                    wi[i] = __fadd_rn(fi[i], ti);
                 } else {
                     const double nr = pr[i] + (double)tr, ni = pi[i] + (double)ti;
                     pr[i] = nr;
@@ -199,12 +194,6 @@ struct EpiHorner {
             }
     }
 };
-
-// Index of the float4 holding states 4 quad .. 4 quad + 3 of row r in the tiled interleaved layout
-// (quads = sp / 4; see the interleaved kernels below).
-__device__ __forceinline__ int64_t il_at(int64_t r, int quad, int quads) {
-    return ((r >> 5) * quads + quad) * 128 + ((r & 31) << 2);
-}
 
 // Renormalisation in float64: per state, partial sums of |psi|^2 over row blocks (fixed order),
 // then every block sums its state's partials and scales its rows; in the mixed mode it also
@@ -287,114 +276,6 @@ __global__ void to_f32_il_kernel(const double *__restrict__ pr, const double *__
     }
 }
 
-// One Taylor term's epilogue for four interleaved states of one row; the arithmetic of EpiMixed.
-struct EpiMixedIL {
-    float *vr, *vi;                 // term out (interleaved)
-    float *hr, *hi_, *lr, *li;      // compensated sum (interleaved)
-    double *pr, *pi;                // state, q at p[q * ld + r]
-    int64_t ld;
-    int sp, nrhs;
-    float scale;
-    int first, last;
-    __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
-        const int64_t i = il_at(r, g, sp >> 2);
-        float tr[4], ti[4], h_r[4], h_i[4], l_r[4], l_i[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            tr[c] = si[c] * scale;
-            ti[c] = -sr[c] * scale;
-        }
-        if (first) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                h_r[c] = tr[c];
-                h_i[c] = ti[c];
-                l_r[c] = l_i[c] = 0.f;
-            }
-        } else {
-            const float4 a = *reinterpret_cast<const float4 *>(hr + i), b = *reinterpret_cast<const float4 *>(hi_ + i);
-            const float4 c4 = *reinterpret_cast<const float4 *>(lr + i), d = *reinterpret_cast<const float4 *>(li + i);
-            const float ha[4] = {a.x, a.y, a.z, a.w}, hb[4] = {b.x, b.y, b.z, b.w};
-            const float la[4] = {c4.x, c4.y, c4.z, c4.w}, lb[4] = {d.x, d.y, d.z, d.w};
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                float e_r, e_i;
-                two_sum(ha[c], tr[c], h_r[c], e_r);
-                two_sum(hb[c], ti[c], h_i[c], e_i);
-                l_r[c] = la[c] + e_r;
-                l_i[c] = lb[c] + e_i;
-            }
-        }
-        if (!last) {
-            *reinterpret_cast<float4 *>(hr + i) = make_float4(h_r[0], h_r[1], h_r[2], h_r[3]);
-            *reinterpret_cast<float4 *>(hi_ + i) = make_float4(h_i[0], h_i[1], h_i[2], h_i[3]);
-            *reinterpret_cast<float4 *>(lr + i) = make_float4(l_r[0], l_r[1], l_r[2], l_r[3]);
-            *reinterpret_cast<float4 *>(li + i) = make_float4(l_i[0], l_i[1], l_i[2], l_i[3]);
-            *reinterpret_cast<float4 *>(vr + i) = make_float4(tr[0], tr[1], tr[2], tr[3]);
-            *reinterpret_cast<float4 *>(vi + i) = make_float4(ti[0], ti[1], ti[2], ti[3]);
-        } else {
-            float nr_[4], ni_[4];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int q = 4 * g + c;
-                nr_[c] = ni_[c] = 0.f;
-                if (q < nrhs) {
-                    const double nr = pr[q * ld + r] + ((double)h_r[c] + (double)l_r[c]);
-                    const double ni = pi[q * ld + r] + ((double)h_i[c] + (double)l_i[c]);
-                    pr[q * ld + r] = nr;
-                    pi[q * ld + r] = ni;
-                    nr_[c] = (float)nr;
-                    ni_[c] = (float)ni;
-                }
-            }
-            *reinterpret_cast<float4 *>(vr + i) = make_float4(nr_[0], nr_[1], nr_[2], nr_[3]);
-            *reinterpret_cast<float4 *>(vi + i) = make_float4(ni_[0], ni_[1], ni_[2], ni_[3]);
-        }
-    }
-};
-
-// The Horner step (EpiHorner) for four interleaved states of one row.
-struct EpiHornerIL {
-    float *wr, *wi;                 // interleaved: w out
-    const float *fr, *fi;           // fp32(psi)
-    float *gr, *gi;                 // fp32(psi) written on the last step
-    double *pr, *pi;                // psi, q at p[q * ld + r]
-    int64_t ld;
-    int sp, nrhs;
-    float scale;
-    int last;
-    __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
-        const int64_t i = il_at(r, g, sp >> 2);
-        float tr[4], ti[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            tr[c] = si[c] * scale;
-            ti[c] = -sr[c] * scale;
-        }
-        if (!last) {
-            const float4 a = *reinterpret_cast<const float4 *>(fr + i), b = *reinterpret_cast<const float4 *>(fi + i);
-            *reinterpret_cast<float4 *>(wr + i) = make_float4(a.x + tr[0], a.y + tr[1], a.z + tr[2], a.w + tr[3]);
-            *reinterpret_cast<float4 *>(wi + i) = make_float4(b.x + ti[0], b.y + ti[1], b.z + ti[2], b.w + ti[3]);
-        } else {
-            float nr_[4], ni_[4];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int q = 4 * g + c;
-                nr_[c] = ni_[c] = 0.f;
-                if (q < nrhs) {
-                    const double nr = pr[q * ld + r] + (double)tr[c], ni = pi[q * ld + r] + (double)ti[c];
-                    pr[q * ld + r] = nr;
-                    pi[q * ld + r] = ni;
-                    nr_[c] = (float)nr;
-                    ni_[c] = (float)ni;
-                }
-            }
-            *reinterpret_cast<float4 *>(gr + i) = make_float4(nr_[0], nr_[1], nr_[2], nr_[3]);
-            *reinterpret_cast<float4 *>(gi + i) = make_float4(ni_[0], ni_[1], ni_[2], ni_[3]);
-        }
-    }
-};
-
 // Thread mapping: warp w of a block takes quad group g = w mod (sp/G) of the 32 rows of row
 // block (block * 8 / (sp/G) + w / (sp/G)); lane l takes row 32 * (that row block) + l.
 //
@@ -423,21 +304,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
 #pragma unroll
     for (int q = 0; q < G; ++q) accr[q] = acci[q] = 0.f;
     auto term = [&](const DiagMeta &m, float a, float b) {
-        const int64_t c = r + m.off;
-#pragma unroll
-        for (int h = 0; h < G / 4; ++h) {
-            const int64_t at = il_at(c, g * (G / 4) + h, quads);
-            const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + at));
-            const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + at));
-            const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                accr[4 * h + q] = fmaf(a, xv[q], accr[4 * h + q]);
-                accr[4 * h + q] = fmaf(-b, yv[q], accr[4 * h + q]);
-                acci[4 * h + q] = fmaf(a, yv[q], acci[4 * h + q]);
-                acci[4 * h + q] = fmaf(b, xv[q], acci[4 * h + q]);
-            }
-        }
+        il_term<G>(r + m.off, g * (G / 4), quads, a, b, xr, xi, accr, acci);
     };
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, nd - c0);

@@ -71,13 +71,15 @@ struct F2 {
 
 // s += a*x for float pairs (see the file comment); sign = -1 subtracts.
 __device__ __forceinline__ void f2_mac(F2 &s, float ah, float al, float xh, float xl, float sign) {
-    const float ph = (sign * ah) * xh;
+    // TwoProd (ph + exact remainder via fma) and TwoSum; the _rn intrinsics keep the compiler from
+    // fusing the product into the sum, which would break both identities
+    const float ph = __fmul_rn(sign * ah, xh);
     float pl = fmaf(sign * ah, xh, -ph);
     pl = fmaf(sign * ah, xl, pl);
     pl = fmaf(sign * al, xh, pl);
-    const float t = s.h + ph;
-    const float bb = t - s.h;
-    const float e = (s.h - (t - bb)) + (ph - bb);
+    const float t = __fadd_rn(s.h, ph);
+    const float bb = __fsub_rn(t, s.h);
+    const float e = __fadd_rn(__fsub_rn(s.h, __fsub_rn(t, bb)), __fsub_rn(ph, bb));
     s.h = t;
     s.l += e + pl;
 }

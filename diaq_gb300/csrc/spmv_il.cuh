@@ -1,0 +1,161 @@
+// Tiled interleaved float32 states and the epilogues that work on them, shared by the evolution
+// plans and the batched form.
+//
+// Layout: rows in blocks of 32, and within a block each quad of 4 states stored as 32 rows x 4
+// floats (512 bytes).  Element (r, q) sits at ((r / 32) * (sp / 4) + q / 4) * 128 + (r mod 32) * 4
+// + q mod 4, sp = the state count rounded up to a power of two >= 4 (padding states zero), rows
+// padded to a multiple of 32.  A warp over 32 consecutive rows and one quad reads its state
+// window at any diagonal offset as one contiguous 512-byte run (one 16-byte load per lane).
+#pragma once
+
+#include "spmv_kernel.cuh"
+
+namespace diaq_gb300 {
+
+// TwoSum (Knuth): s + e = a + b exactly, s = fl(a + b).  The _rn intrinsics keep the compiler
+// from fusing an add with the multiply that produced b, which would break the identity.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Index of the float4 holding states 4 quad .. 4 quad + 3 of row r in the tiled interleaved layout
+// (quads = sp / 4).
+__device__ __forceinline__ int64_t il_at(int64_t r, int quad, int quads) {
+    return ((r >> 5) * quads + quad) * 128 + ((r & 31) << 2);
+}
+
+// One Taylor term's epilogue for four interleaved states of one row; the arithmetic of EpiMixed.
+struct EpiMixedIL {
+    float *vr, *vi;                 // term out (interleaved)
+    float *hr, *hi_, *lr, *li;      // compensated sum (interleaved)
+    double *pr, *pi;                // state, q at p[q * ld + r]
+    int64_t ld;
+    int sp, nrhs;
+    float scale;
+    int first, last;
+    __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
+        const int64_t i = il_at(r, g, sp >> 2);
+        float tr[4], ti[4], h_r[4], h_i[4], l_r[4], l_i[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tr[c] = si[c] * scale;
+            ti[c] = -sr[c] * scale;
+        }
+        if (first) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                h_r[c] = tr[c];
+                h_i[c] = ti[c];
+                l_r[c] = l_i[c] = 0.f;
+            }
+        } else {
+            const float4 a = *reinterpret_cast<const float4 *>(hr + i), b = *reinterpret_cast<const float4 *>(hi_ + i);
+            const float4 c4 = *reinterpret_cast<const float4 *>(lr + i), d = *reinterpret_cast<const float4 *>(li + i);
+            const float ha[4] = {a.x, a.y, a.z, a.w}, hb[4] = {b.x, b.y, b.z, b.w};
+            const float la[4] = {c4.x, c4.y, c4.z, c4.w}, lb[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float e_r, e_i;
+                two_sum(ha[c], tr[c], h_r[c], e_r);
+                two_sum(hb[c], ti[c], h_i[c], e_i);
+                l_r[c] = la[c] + e_r;
+                l_i[c] = lb[c] + e_i;
+            }
+        }
+        if (!last) {
+            *reinterpret_cast<float4 *>(hr + i) = make_float4(h_r[0], h_r[1], h_r[2], h_r[3]);
+            *reinterpret_cast<float4 *>(hi_ + i) = make_float4(h_i[0], h_i[1], h_i[2], h_i[3]);
+            *reinterpret_cast<float4 *>(lr + i) = make_float4(l_r[0], l_r[1], l_r[2], l_r[3]);
+            *reinterpret_cast<float4 *>(li + i) = make_float4(l_i[0], l_i[1], l_i[2], l_i[3]);
+            *reinterpret_cast<float4 *>(vr + i) = make_float4(tr[0], tr[1], tr[2], tr[3]);
+            *reinterpret_cast<float4 *>(vi + i) = make_float4(ti[0], ti[1], ti[2], ti[3]);
+        } else {
+            float nr_[4], ni_[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int q = 4 * g + c;
+                nr_[c] = ni_[c] = 0.f;
+                if (q < nrhs) {
+                    const double nr = pr[q * ld + r] + ((double)h_r[c] + (double)l_r[c]);
+                    const double ni = pi[q * ld + r] + ((double)h_i[c] + (double)l_i[c]);
+                    pr[q * ld + r] = nr;
+                    pi[q * ld + r] = ni;
+                    nr_[c] = (float)nr;
+                    ni_[c] = (float)ni;
+                }
+            }
+            *reinterpret_cast<float4 *>(vr + i) = make_float4(nr_[0], nr_[1], nr_[2], nr_[3]);
+            *reinterpret_cast<float4 *>(vi + i) = make_float4(ni_[0], ni_[1], ni_[2], ni_[3]);
+        }
+    }
+};
+
+// The Horner step (EpiHorner) for four interleaved states of one row.
+struct EpiHornerIL {
+    float *wr, *wi;                 // interleaved: w out
+    const float *fr, *fi;           // fp32(psi)
+    float *gr, *gi;                 // fp32(psi) written on the last step
+    double *pr, *pi;                // psi, q at p[q * ld + r]
+    int64_t ld;
+    int sp, nrhs;
+    float scale;
+    int last;
+    __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
+        const int64_t i = il_at(r, g, sp >> 2);
+        float tr[4], ti[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tr[c] = si[c] * scale;
+            ti[c] = -sr[c] * scale;
+        }
+        if (!last) {
+            const float4 a = *reinterpret_cast<const float4 *>(fr + i), b = *reinterpret_cast<const float4 *>(fi + i);
+            // unfused (rounded product, then rounded sum): the planar kernels give the same bits
+            *reinterpret_cast<float4 *>(wr + i) = make_float4(__fadd_rn(a.x, tr[0]), __fadd_rn(a.y, tr[1]),
+                                                              __fadd_rn(a.z, tr[2]), __fadd_rn(a.w, tr[3]));
+            *reinterpret_cast<float4 *>(wi + i) = make_float4(__fadd_rn(b.x, ti[0]), __fadd_rn(b.y, ti[1]),
+                                                              __fadd_rn(b.z, ti[2]), __fadd_rn(b.w, ti[3]));
+        } else {
+            float nr_[4], ni_[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int q = 4 * g + c;
+                nr_[c] = ni_[c] = 0.f;
+                if (q < nrhs) {
+                    const double nr = pr[q * ld + r] + (double)tr[c], ni = pi[q * ld + r] + (double)ti[c];
+                    pr[q * ld + r] = nr;
+                    pi[q * ld + r] = ni;
+                    nr_[c] = (float)nr;
+                    ni_[c] = (float)ni;
+                }
+            }
+            *reinterpret_cast<float4 *>(gr + i) = make_float4(nr_[0], nr_[1], nr_[2], nr_[3]);
+            *reinterpret_cast<float4 *>(gi + i) = make_float4(ni_[0], ni_[1], ni_[2], ni_[3]);
+        }
+    }
+};
+
+// One diagonal's contribution to G states (G / 4 quads from quad g0) of row r: the state window
+// at column c = r + off, two 16-byte loads per quad.
+template <int G>
+__device__ __forceinline__ void il_term(int64_t c, int g0, int quads, float a, float b, const float *__restrict__ xr,
+                                        const float *__restrict__ xi, float (&accr)[G], float (&acci)[G]) {
+#pragma unroll
+    for (int h = 0; h < G / 4; ++h) {
+        const int64_t at = il_at(c, g0 + h, quads);
+        const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + at));
+        const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + at));
+        const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            accr[4 * h + q] = fmaf(a, xv[q], accr[4 * h + q]);
+            accr[4 * h + q] = fmaf(-b, yv[q], accr[4 * h + q]);
+            acci[4 * h + q] = fmaf(a, yv[q], acci[4 * h + q]);
+            acci[4 * h + q] = fmaf(b, xv[q], acci[4 * h + q]);
+        }
+    }
+}
+
+}  // namespace diaq_gb300

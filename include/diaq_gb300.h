@@ -320,6 +320,12 @@ int diaq_batch_config(diaq_batch_t B, int *states_per_launch, int *rows_per_thre
  * Drops the recorded step. */
 int diaq_batch_set_horner(diaq_batch_t B, int on);
 
+/* on != 0 (the default): complex64 instances with 4 to 32 states keep their float32 work vectors
+ * interleaved in tiles of 32 rows x 4 states and run in a second kernel per phase, one block per
+ * block of rows and all the states; off: every instance planar.  Same arithmetic either way.
+ * Drops the recorded step. */
+int diaq_batch_set_interleaved(diaq_batch_t B, int on);
+
 /* ------------------------------------------------------------------------------------------
  * The learned (s, m) proposer: an FP32 MLP 16 -> 64 -> 64 -> 21 + 30 logits (ReLU), trained
  * with softmax cross-entropy on both heads (s in 0..20, m in 1..30) and Adam.  No counterpart in

@@ -101,3 +101,35 @@ def test_batched_autotune_keeps_states(native, tmp_path, monkeypatch):
     want = orc.ham_sim(oms[0], P0[0][0], 0.04, 2, 10)
     assert np.linalg.norm(got[0] - want) / np.linalg.norm(want) < 1e-6
     assert (tmp_path / "tune.json").exists()
+
+
+IL_SPECS = [("xxz", 11, 4, 1), ("tfim", 10, 5, 2), ("xxz", 9, 8, 3), ("tfim", 8, 16, 4), ("xxz", 7, 32, 5),
+            ("tfim", 3, 6, 6), ("xxz", 6, 33, 7), ("tfim", 9, 1, 8), ("xxz", 5, 3, 9)]
+
+
+@pytest.mark.parametrize("horner", [False, True])
+def test_batched_interleaved_matches_planar_and_oracle(native, horner):
+    """complex64 instances with 4-32 states run interleaved (8 or 4 states per thread, rows
+    padded to 32: the 3-qubit instance has 8 rows), the rest planar; the same arithmetic in the
+    same order, so both layouts give the same bits, and both match the oracle."""
+    import torch
+
+    capi, _ = native
+    s = [0, 1, 0, 0, 1, 0, 0, 2, 0]
+    m = [9, 7, 12, 6, 5, 11, 8, 3, 10]
+    out = {}
+    for il in (True, False):
+        mats, oms, prs, pis, P0 = _make(capi, IL_SPECS, 1)
+        B = capi.Batch(mats, prs, pis)
+        B.set_horner(horner)
+        B.set_interleaved(il)
+        B.set_config(4, 2)
+        B.run(0.02, s, m, 3)
+        torch.cuda.synchronize()
+        out[il] = [(p + 1j * q).cpu().numpy() for p, q in zip(prs, pis)]
+    for i, A in enumerate(oms):
+        assert np.array_equal(out[True][i], out[False][i]), i
+        for q in range(P0[i].shape[0]):
+            want = orc.ham_sim(A, P0[i][q], 0.06, 3, m[i], substeps=1 << s[i])
+            err = np.linalg.norm(out[True][i][q] - want) / np.linalg.norm(want)
+            assert err < 1e-6, (i, q, err)
