@@ -55,6 +55,8 @@ struct BatchInst {
     int il_ok, il;   // may use / uses the interleaved layout
     int sp;          // interleaved: states padded to a power of two >= 4
     int64_t n_pad;   // interleaved: rows padded to a multiple of 32
+    const uint32_t *tmask;  // zero-tile mask of the matrix (rebuilt at every run), mw words per diagonal
+    int64_t mw;
     double tau;      // dt / 2^s
     double *pr, *pi; // states, leading dimension rows
     void *var, *vai, *vbr, *vbi, *hr, *hi, *lr, *li;  // T work vectors, leading dimension rows
@@ -80,6 +82,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
     batched_phase_kernel(const BatchInst *__restrict__ insts, const BatchItem *__restrict__ items, int n_items,
                          int phase) {
     __shared__ DiagMeta sm[kMetaChunk];
+    __shared__ uint32_t smk[kMetaChunk];
     __shared__ BatchInst si;
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
         const BatchItem item = items[it];
@@ -138,12 +141,18 @@ __global__ void __launch_bounds__(kSpmvThreads)
         for (int c0 = 0; c0 < I.nd; c0 += kMetaChunk) {
             const int cn = min(kMetaChunk, I.nd - c0);
             __syncthreads();
-            for (int j = threadIdx.x; j < cn; j += kSpmvThreads) sm[j] = I.meta[c0 + j];
+            // the item's 256 VR rows (VR | 4) lie in one 1024-row mask word, a thread's VR in one tile
+            const int64_t mword = ((int64_t)item.tile * kSpmvThreads * VR) >> 10;
+            for (int j = threadIdx.x; j < cn; j += kSpmvThreads) {
+                sm[j] = I.meta[c0 + j];
+                smk[j] = I.tmask[(int64_t)(c0 + j) * I.mw + mword];
+            }
             __syncthreads();
             if (r0 >= I.rows) continue;
+            const int tbit = (int)((r0 >> 5) & 31);
             for (int j = 0; j < cn; ++j) {
                 const int64_t lo = sm[j].lo, hi = sm[j].hi;
-                if (r0 + VR <= lo || r0 >= hi) continue;
+                if (r0 + VR <= lo || r0 >= hi || !((smk[j] >> tbit) & 1u)) continue;
                 const int64_t base = sm[j].base, c = r0 + sm[j].off;
                 T ar[VR], ai[VR];
                 load_vec_stream<T, VR>(ar, are + base + r0);
@@ -255,7 +264,8 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // states.  Phases as in batched_phase_kernel; the initialisation and copy phases move the item's
 // rows of every state, which are one contiguous range of the tiled vectors.
 template <int G>
-__device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm, int64_t tile, int phase) {
+__device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm, uint32_t *smk, int64_t tile,
+                                                int phase) {
     const int quads = I.sp >> 2, groups = I.sp / G;
     const int64_t rpb = 32 * (8 / groups);
     const int64_t r0 = tile * rpb, ld = I.rows;
@@ -306,12 +316,16 @@ __device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm
     for (int c0 = 0; c0 < I.nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, I.nd - c0);
         __syncthreads();
-        for (int j = threadIdx.x; j < cn; j += kSpmvThreads) sm[j] = I.meta[c0 + j];
+        for (int j = threadIdx.x; j < cn; j += kSpmvThreads) {
+            sm[j] = I.meta[c0 + j];
+            smk[j] = I.tmask[(int64_t)(c0 + j) * I.mw + (r0 >> 10)];  // the item's <= 256 rows: one word
+        }
         __syncthreads();
         if (r >= I.rows) continue;
+        const int tbit = (int)((r >> 5) & 31);
 #pragma unroll 4
         for (int j = 0; j < cn; ++j) {
-            if (r < sm[j].lo || r >= sm[j].hi) continue;
+            if (r < sm[j].lo || r >= sm[j].hi || !((smk[j] >> tbit) & 1u)) continue;
             il_term<G>(r + sm[j].off, g * (G / 4), quads, __ldcs(are + sm[j].base + r), __ldcs(aim + sm[j].base + r), xr,
                        xi, accr, acci);
         }
@@ -344,11 +358,12 @@ template <int G>
 __global__ void __launch_bounds__(kSpmvThreads, 4)
     batched_il_kernel(const BatchInst *__restrict__ insts, const BatchItem *__restrict__ items, int phase) {
     __shared__ DiagMeta sm[kMetaChunk];
+    __shared__ uint32_t smk[kMetaChunk];
     __shared__ BatchInst si;
     const BatchItem item = items[blockIdx.x];
     if (threadIdx.x == 0) si = insts[item.inst];
     __syncthreads();
-    batched_il_item<G>(si, sm, item.tile, phase);
+    batched_il_item<G>(si, sm, smk, item.tile, phase);
 }
 
 struct Batch {
@@ -363,6 +378,8 @@ struct Batch {
     bool il_on = true;                // interleave the instances that can be
     int items_il = -1;                // il_on of the current item lists
     void *work = nullptr;
+    uint32_t *masks = nullptr;        // zero-tile masks of every instance's matrix
+    std::vector<const Matrix *> mats;
     cudaStream_t s = nullptr;         // capture stream
     SpmvCfg cfg{8, 0};
     bool tuned = false;
@@ -379,6 +396,7 @@ struct Batch {
         cudaFree(d_items);
         cudaFree(d_il_items);
         cudaFree(work);
+        cudaFree(masks);
         if (s) cudaStreamDestroy(s);
     }
 };
@@ -694,12 +712,16 @@ int diaq_batch_create(int n_inst, const diaq_matrix_t *H, const int *nrhs, doubl
     B->prec = prec;
     cudaError_t e = cudaStreamCreateWithFlags(&B->s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&B->work, work_bytes + 256);
+    size_t mask_words = 0;
+    for (int i = 0; i < n_inst; ++i) mask_words += (size_t)H[i]->nd * (size_t)tile_mask_words(H[i]->rows);
+    if (e == cudaSuccess) e = cudaMalloc(&B->masks, sizeof(uint32_t) * std::max<size_t>(mask_words, 1));
     if (e == cudaSuccess) e = cudaMalloc(&B->d_inst, sizeof(BatchInst) * n_inst);
     if (e != cudaSuccess) {
         delete B;
         return cuda_status(e, "batch create", __FILE__, __LINE__);
     }
     uint8_t *w = (uint8_t *)B->work;
+    size_t mask_off = 0;
     for (int i = 0; i < n_inst; ++i) {
         BatchInst I{};
         I.meta = H[i]->d_meta;
@@ -711,6 +733,10 @@ int diaq_batch_create(int n_inst, const diaq_matrix_t *H, const int *nrhs, doubl
         I.pr = psi_re[i];
         I.pi = psi_im[i];
         I.il_ok = il_shape(i, I.sp, I.n_pad) ? 1 : 0;
+        I.tmask = B->masks + mask_off;
+        I.mw = tile_mask_words(H[i]->rows);
+        mask_off += (size_t)H[i]->nd * (size_t)I.mw;
+        B->mats.push_back(H[i]);
         const size_t vb = vec_bytes(i);
         void **slots[8] = {&I.var, &I.vai, &I.vbr, &I.vbi, &I.hr, &I.hi, &I.lr, &I.li};
         for (int j = 0; j < 8; ++j) {
@@ -778,6 +804,8 @@ int diaq_batch_run(diaq_batch_t B, double dt, const int *substeps_log2, const in
     if (!B || !substeps_log2 || !m || steps < 0) return set_error(DIAQ_ERR_INVALID, "batch run: bad argument");
     if (steps == 0) return DIAQ_OK;
     cudaStream_t user = (cudaStream_t)stream;
+    // the matrices are the caller's: their zero-tile masks are taken afresh at every run
+    for (size_t i = 0; i < B->inst.size(); ++i) DQ_TRY(build_tile_mask(*B->mats[i], (uint32_t *)B->inst[i].tmask, user));
     DQ_CUDA(cudaStreamSynchronize(user));
     std::vector<int> key(substeps_log2, substeps_log2 + B->inst.size());
     key.insert(key.end(), m, m + B->inst.size());

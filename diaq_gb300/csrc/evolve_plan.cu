@@ -293,13 +293,16 @@ template <class Epi, int D, int G = 4>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_il_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                        const float *__restrict__ aim, int64_t rows, const float *__restrict__ xr,
-                       const float *__restrict__ xi, Epi epi) {
+                       const float *__restrict__ xi, const uint32_t *__restrict__ tmask, int64_t mw, Epi epi) {
     static_assert(G == 4 || G == 8, "4 or 8 states per thread");
     __shared__ DiagMeta sm[kMetaChunk];
+    __shared__ uint32_t smk[kMetaChunk];  // zero-tile mask word of the block rows, per diagonal
     const int quads = epi.sp >> 2, groups = epi.sp / G;
     const int wid = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
     const int g = wid % groups;
-    const int64_t r = ((int64_t)blockIdx.x * (8 / groups) + wid / groups) * 32 + lane;
+    const int64_t row0 = (int64_t)blockIdx.x * (8 / groups) * 32;  // <= 256 rows: one mask word
+    const int64_t r = row0 + (wid / groups) * 32 + lane;
+    const int tbit = (int)((r >> 5) & 31);
     float accr[G], acci[G];
 #pragma unroll
     for (int q = 0; q < G; ++q) accr[q] = acci[q] = 0.f;
@@ -309,13 +312,18 @@ __global__ void __launch_bounds__(kSpmvThreads)
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, nd - c0);
         __syncthreads();
-        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
+        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) {
+            sm[i] = meta[c0 + i];
+            smk[i] = tmask ? tmask[(int64_t)(c0 + i) * mw + (row0 >> 10)] : 0xffffffffu;
+        }
         __syncthreads();
         if (r >= rows) continue;
+        // a warp's 32 rows are one tile: the whole warp skips a zero tile
+        auto live = [&](int k) { return r >= sm[k].lo && r < sm[k].hi && ((smk[k] >> tbit) & 1u); };
         if constexpr (D == 0) {
 #pragma unroll 4
             for (int k = 0; k < cn; ++k) {
-                if (r < sm[k].lo || r >= sm[k].hi) continue;
+                if (!live(k)) continue;
                 term(sm[k], __ldcs(are + sm[k].base + r), __ldcs(aim + sm[k].base + r));
             }
         } else {
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
             float ra[D], rb[D];
 #pragma unroll
             for (int d = 0; d < D; ++d) {
-                const bool in = d < cn && r >= sm[d].lo && r < sm[d].hi;
+                const bool in = d < cn && live(d);
                 ra[d] = in ? __ldcs(are + sm[d].base + r) : 0.f;
                 rb[d] = in ? __ldcs(aim + sm[d].base + r) : 0.f;
             }
@@ -334,10 +342,10 @@ __global__ void __launch_bounds__(kSpmvThreads)
                     if (k < cn) {
                         const float a = ra[d], b = rb[d];
                         const int kn = k + D;
-                        const bool in = kn < cn && r >= sm[kn].lo && r < sm[kn].hi;
+                        const bool in = kn < cn && live(kn);
                         ra[d] = in ? __ldcs(are + sm[kn].base + r) : 0.f;
                         rb[d] = in ? __ldcs(aim + sm[kn].base + r) : 0.f;
-                        if (r >= sm[k].lo && r < sm[k].hi) term(sm[k], a, b);
+                        if (live(k)) term(sm[k], a, b);
                     }
                 }
             }
@@ -375,6 +383,7 @@ struct EvolvePlan {
     bool tuned = false;   // cfg chosen (by the autotuner or the caller)
     bool renorm = false;  // rescale every state to norm 1 (float64) after each step
     double *part = nullptr;  // renormalisation partial sums, nrhs * kNormBlocks
+    uint32_t *tmask = nullptr;  // zero-tile mask of the matrix the term kernels read (Hc, or H for C128)
     int sp = 4;           // interleaved layout: nrhs rounded up to a power of two >= 4 (<= 32 used)
     int64_t n_pad = 0;    // rows rounded up to a multiple of 32
 
@@ -387,6 +396,7 @@ struct EvolvePlan {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
         if (buf) cudaFree(buf);
         if (part) cudaFree(part);
+        if (tmask) cudaFree(tmask);
         if (Hc) destroy(Hc);
         if (s) cudaStreamDestroy(s);
     }
@@ -411,14 +421,16 @@ int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &
     const float *are = (const float *)P.Hc->re, *aim = (const float *)P.Hc->im;
     const DiagMeta *md = P.Hc->d_meta;
     const int nd = P.Hc->nd;
+    const uint32_t *tm = P.tmask;
+    const int64_t mw = tile_mask_words(P.n);
     if (eight)
-        dia_spmv_il_kernel<Epi, 0, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+        dia_spmv_il_kernel<Epi, 0, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, tm, mw, e);
     else if (v == 7)
-        dia_spmv_il_kernel<Epi, 4><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+        dia_spmv_il_kernel<Epi, 4><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, tm, mw, e);
     else if (v == 8)
-        dia_spmv_il_kernel<Epi, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+        dia_spmv_il_kernel<Epi, 8><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, tm, mw, e);
     else
-        dia_spmv_il_kernel<Epi, 0><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, e);
+        dia_spmv_il_kernel<Epi, 0><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, tm, mw, e);
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;
 }
@@ -447,6 +459,15 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     if (e == cudaSuccess && bytes) e = cudaMalloc(&P->buf, bytes);
     if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
     if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
+    if (st == DIAQ_OK && H.nd > 0) {
+        // the mask of the plan's own c64 copy is built once; that of the caller's c128 matrix
+        // again at every run (its values may have changed)
+        e = cudaMalloc(&P->tmask, sizeof(uint32_t) * (size_t)H.nd * (size_t)tile_mask_words(H.rows));
+        if (e != cudaSuccess) st = cuda_status(e, "evolve plan mask", __FILE__, __LINE__);
+        if (st == DIAQ_OK) st = build_tile_mask(P->Hc ? *P->Hc : H, P->tmask, P->s);
+        if (st == DIAQ_OK && (e = cudaStreamSynchronize(P->s)) != cudaSuccess)
+            st = cuda_status(e, "evolve plan mask", __FILE__, __LINE__);
+    }
     if (st != DIAQ_OK) {
         delete static_cast<diaq_evolve_s *>(P);
         return st;
@@ -502,7 +523,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
                 e.outi = oth_i;
                 e.ld = L;
                 e.scale = tau / (double)t;
-                DQ_TRY((launch_dia_spmv_rhs_cfg<double, EpiPlain, 2, 1>(*P.H, tin_r, tin_i, L, (int)k, e, P.s, P.cfg)));
+                DQ_TRY((launch_dia_spmv_rhs_cfg<double, EpiPlain, 2, 1>(*P.H, tin_r, tin_i, L, (int)k, e, P.s, P.cfg, P.tmask)));
                 ++P.launches_per_step;
                 tin_r = tout_r;
                 tin_i = tout_i;
@@ -539,7 +560,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
                 } else {
                     EpiHorner e{out_r, out_i, fr, fi, pr, pi, gr, gi, L, scale, last};
                     DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiHorner, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s,
-                                                                            P.cfg)));
+                                                                            P.cfg, P.tmask)));
                 }
                 ++P.launches_per_step;
                 if (gr != fr) {
@@ -592,7 +613,7 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
                 DQ_TRY(launch_dia_spmv_pipe<EpiMixed>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg.kmax,
                                                       &P.launches_per_step));
             } else {
-                DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiMixed, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg)));
+                DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiMixed, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s, P.cfg, P.tmask)));
                 ++P.launches_per_step;  // one launch over all states
             }
             std::swap(in_r, out_r);
@@ -782,6 +803,7 @@ static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt
     if (steps < 0 || m < 0 || sl < 0 || sl > 20) return set_error(DIAQ_ERR_INVALID, "evolve: bad steps / s / m");
     if (!pr || !pi) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
     if (steps == 0 || m == 0 || P.n == 0) return DIAQ_OK;
+    if (!P.Hc && P.tmask) DQ_TRY(build_tile_mask(*P.H, P.tmask, user));
     DQ_TRY(ensure_renorm_buffer(P));
     if (!P.tuned) DQ_TRY(autotune(P, dt, sl, m, pr, pi, ld, user));
     const EvolvePlan::Key key{dt, sl, m, pr, pi, ld};

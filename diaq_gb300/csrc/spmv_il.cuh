@@ -137,17 +137,28 @@ struct EpiHornerIL {
     }
 };
 
-// One diagonal's contribution to G states (G / 4 quads from quad g0) of row r: the state window
-// at column c = r + off, two 16-byte loads per quad.
+// The state window of G states (G / 4 quads from quad g0) at column c: two 16-byte loads per quad.
 template <int G>
-__device__ __forceinline__ void il_term(int64_t c, int g0, int quads, float a, float b, const float *__restrict__ xr,
-                                        const float *__restrict__ xi, float (&accr)[G], float (&acci)[G]) {
+struct IlWindow {
+    float4 x[G / 4], y[G / 4];
+};
+template <int G>
+__device__ __forceinline__ void il_load(int64_t c, int g0, int quads, const float *__restrict__ xr,
+                                        const float *__restrict__ xi, IlWindow<G> &w) {
 #pragma unroll
     for (int h = 0; h < G / 4; ++h) {
         const int64_t at = il_at(c, g0 + h, quads);
-        const float4 x = __ldg(reinterpret_cast<const float4 *>(xr + at));
-        const float4 y = __ldg(reinterpret_cast<const float4 *>(xi + at));
-        const float xv[4] = {x.x, x.y, x.z, x.w}, yv[4] = {y.x, y.y, y.z, y.w};
+        w.x[h] = __ldg(reinterpret_cast<const float4 *>(xr + at));
+        w.y[h] = __ldg(reinterpret_cast<const float4 *>(xi + at));
+    }
+}
+// acc += (a + i b) * window, per state
+template <int G>
+__device__ __forceinline__ void il_fma(float a, float b, const IlWindow<G> &w, float (&accr)[G], float (&acci)[G]) {
+#pragma unroll
+    for (int h = 0; h < G / 4; ++h) {
+        const float xv[4] = {w.x[h].x, w.x[h].y, w.x[h].z, w.x[h].w};
+        const float yv[4] = {w.y[h].x, w.y[h].y, w.y[h].z, w.y[h].w};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             accr[4 * h + q] = fmaf(a, xv[q], accr[4 * h + q]);
@@ -156,6 +167,15 @@ __device__ __forceinline__ void il_term(int64_t c, int g0, int quads, float a, f
             acci[4 * h + q] = fmaf(b, xv[q], acci[4 * h + q]);
         }
     }
+}
+
+// One diagonal's contribution to G states of row r, window at column c = r + off.
+template <int G>
+__device__ __forceinline__ void il_term(int64_t c, int g0, int quads, float a, float b, const float *__restrict__ xr,
+                                        const float *__restrict__ xi, float (&accr)[G], float (&acci)[G]) {
+    IlWindow<G> w;
+    il_load<G>(c, g0, quads, xr, xi, w);
+    il_fma<G>(a, b, w, accr, acci);
 }
 
 }  // namespace diaq_gb300

@@ -20,6 +20,18 @@ namespace diaq_gb300 {
 constexpr int kSpmvThreads = 256;
 constexpr int kMetaChunk = 256;
 
+// ---- zero-tile mask --------------------------------------------------------------------------------
+// One bit per diagonal and 32-row tile: bit t of word w of diagonal j is set when rows
+// 32 (32 w + t) .. 32 (32 w + t) + 31 of diagonal j hold a nonzero value (real or imaginary part),
+// word (j, w) at mask[j * tile_mask_words(rows) + w].  Kernels whose warps cover aligned 32-row
+// tiles skip a clear tile whole -- no matrix load, no state window, no multiply-adds.  In
+// Pauli-sum Hamiltonians most off-diagonal tiles are zero: the hopping term of qubits k, k+1
+// fills a quarter of the rows of its diagonal, in runs of 2^k rows.  Leaving out terms a * x
+// with a == 0 changes no finite sum (up to the sign of a zero result).
+inline int64_t tile_mask_words(int64_t rows) { return (rows + 1023) / 1024; }
+// Fill the mask of A (tile_mask_words(A.rows) * A.nd words) on stream s.
+int build_tile_mask(const Matrix &A, uint32_t *mask, cudaStream_t s);
+
 // VR consecutive values of T as one aligned vector load (VR * sizeof(T) bytes).
 template <typename T, int VR>
 struct Vec;
@@ -93,10 +105,12 @@ template <typename T, int K, int VR, class Epi>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_spmv_kernel(const DiagMeta *__restrict__ meta, int nd, const T *__restrict__ are,
                     const T *__restrict__ aim, int64_t rows, const T *__restrict__ xr,
-                    const T *__restrict__ xi, int64_t ldx, int nrhs, int nchunk, Epi epi0) {
+                    const T *__restrict__ xi, int64_t ldx, int nrhs, int nchunk, const uint32_t *__restrict__ tmask,
+                    int64_t mw, Epi epi0) {
     constexpr int V = VR;
     constexpr int VB = VR * (int)sizeof(T);
     __shared__ DiagMeta sm[kMetaChunk];
+    __shared__ uint32_t smk[kMetaChunk];  // zero-tile mask word of the block rows, per diagonal
     const int chunk = (int)(blockIdx.x % (unsigned)nchunk);
     const int64_t tile = blockIdx.x / (unsigned)nchunk;
     const int q0 = chunk * K;
@@ -105,6 +119,9 @@ __global__ void __launch_bounds__(kSpmvThreads)
     xi += q0 * ldx;
     const Epi epi = epi0.shifted(q0);
     const int64_t r0 = (tile * kSpmvThreads + threadIdx.x) * V;
+    // a block's 256 V rows (V | 4) lie in one 1024-row mask word; a thread's V rows in one tile
+    const int64_t mword = (tile * kSpmvThreads * V) >> 10;
+    const int tbit = (int)((r0 >> 5) & 31);
     T accr[K][V], acci[K][V];
 #pragma unroll
     for (int q = 0; q < K; ++q)
@@ -114,13 +131,16 @@ __global__ void __launch_bounds__(kSpmvThreads)
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, nd - c0);
         __syncthreads();
-        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
+        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) {
+            sm[i] = meta[c0 + i];
+            smk[i] = tmask ? tmask[(int64_t)(c0 + i) * mw + mword] : 0xffffffffu;
+        }
         __syncthreads();
         if (r0 >= rows) continue;
 #pragma unroll 2
         for (int k = 0; k < cn; ++k) {
             const int64_t lo = sm[k].lo, hi = sm[k].hi;
-            if (r0 + V <= lo || r0 >= hi) continue;
+            if (r0 + V <= lo || r0 >= hi || !((smk[k] >> tbit) & 1u)) continue;
             const int64_t base = sm[k].base;
             const int64_t d = sm[k].off;
             T ar[V], ai[V];
@@ -418,25 +438,27 @@ struct SpmvCfg {
 
 template <typename T, int K, class Epi, int VR, int... More>
 void launch_vr(int vr, const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, int nchunk,
-               const Epi &e, cudaStream_t s) {
+               const Epi &e, cudaStream_t s, const uint32_t *tmask) {
     if constexpr (sizeof...(More) > 0) {
         if (vr != VR) {
-            launch_vr<T, K, Epi, More...>(vr, A, xr, xi, ldx, nrhs, nchunk, e, s);
+            launch_vr<T, K, Epi, More...>(vr, A, xr, xi, ldx, nrhs, nchunk, e, s, tmask);
             return;
         }
     }
     dia_spmv_kernel<T, K, VR, Epi><<<spmv_blocks(A.rows, VR) * (unsigned)nchunk, kSpmvThreads, 0, s>>>(
-        A.d_meta, A.nd, (const T *)A.re, (const T *)A.im, A.rows, xr, xi, ldx, nrhs, nchunk, e);
+        A.d_meta, A.nd, (const T *)A.re, (const T *)A.im, A.rows, xr, xi, ldx, nrhs, nchunk, tmask,
+        tile_mask_words(A.rows), e);
 }
 
 // One launch over all right-hand sides, in chunks of up to cfg.kmax (<= 8) states per block
 // (the kernel instantiated for 1, 2, 4 or 8 states, unused slots of the last chunk masked); the
 // chunks of a row tile run side by side (see dia_spmv_kernel).  VRs lists the rows-per-thread
 // variants compiled for this epilogue (the first is the default).  Epi must offer
-// `shifted(q0)` on host and device, the same epilogue for right-hand sides q0.. .
+// `shifted(q0)` on host and device, the same epilogue for right-hand sides q0.. .  tmask: A's
+// zero-tile mask (build_tile_mask), or NULL to visit every tile.
 template <typename T, class Epi, int... VRs>
 int launch_dia_spmv_rhs_cfg(const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, Epi epi,
-                            cudaStream_t s, SpmvCfg cfg) {
+                            cudaStream_t s, SpmvCfg cfg, const uint32_t *tmask = nullptr) {
     if (A.rows == 0 || nrhs <= 0) return DIAQ_OK;
     int k = cfg.kmax >= 8 ? 8 : cfg.kmax >= 4 ? 4 : cfg.kmax >= 2 ? 2 : 1;
     while (k > 1 && k / 2 >= nrhs) k /= 2;  // no wider than the states need
@@ -445,13 +467,13 @@ int launch_dia_spmv_rhs_cfg(const Matrix &A, const T *xr, const T *xi, int64_t l
     if ((uint64_t)spmv_blocks(A.rows, vr) * (uint64_t)nchunk > 0x7fffffffull)
         return set_error(DIAQ_ERR_UNSUPPORTED, "spmv: too many row tiles x state chunks for one launch");
     if (k == 8)
-        launch_vr<T, 8, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s);
+        launch_vr<T, 8, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s, tmask);
     else if (k == 4)
-        launch_vr<T, 4, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s);
+        launch_vr<T, 4, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s, tmask);
     else if (k == 2)
-        launch_vr<T, 2, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s);
+        launch_vr<T, 2, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s, tmask);
     else
-        launch_vr<T, 1, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s);
+        launch_vr<T, 1, Epi, VRs...>(vr, A, xr, xi, ldx, nrhs, nchunk, epi, s, tmask);
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;
 }

@@ -1,0 +1,48 @@
+// Zero-tile masks of device matrices (the layout is described with tile_mask_words in
+// spmv_kernel.cuh).  One block per (1024-row word, diagonal): each warp tests four 32-row tiles
+// with a ballot, the block ORs the bits into one word.  Reads every stored value once.
+#include <algorithm>
+
+#include "spmv_kernel.cuh"
+
+namespace diaq_gb300 {
+
+template <typename T>
+__global__ void tile_mask_kernel(const DiagMeta *__restrict__ meta, int nd, const T *__restrict__ re,
+                                 const T *__restrict__ im, int64_t W, uint32_t *__restrict__ mask) {
+    __shared__ uint32_t word;
+    const int lane = (int)threadIdx.x & 31, warp = (int)threadIdx.x >> 5;
+    const int64_t w = blockIdx.x;
+    for (int j = blockIdx.y; j < nd; j += gridDim.y) {
+        __syncthreads();  // the previous diagonal's word is stored
+        if (threadIdx.x == 0) word = 0u;
+        __syncthreads();
+        const DiagMeta m = meta[j];
+        for (int t = warp; t < 32; t += (int)(blockDim.x >> 5)) {
+            const int64_t r = (w * 32 + t) * 32 + lane;
+            bool nz = false;
+            if (r >= m.lo && r < m.hi) nz = re[m.base + r] != (T)0 || im[m.base + r] != (T)0;
+            const unsigned any = __ballot_sync(0xffffffffu, nz);
+            if (any && lane == 0) atomicOr(&word, 1u << t);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) mask[(int64_t)j * W + w] = word;
+    }
+}
+
+int build_tile_mask(const Matrix &A, uint32_t *mask, cudaStream_t s) {
+    if (A.nd == 0 || A.rows == 0) return DIAQ_OK;
+    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "tile mask: c128 or c64 matrices only");
+    const int64_t W = tile_mask_words(A.rows);
+    if (W > 0x7fffffffll) return set_error(DIAQ_ERR_UNSUPPORTED, "tile mask: too many rows");
+    const dim3 grid((unsigned)W, (unsigned)std::min(A.nd, 65535));
+    if (A.prec == DIAQ_C64)
+        tile_mask_kernel<float><<<grid, 256, 0, s>>>(A.d_meta, A.nd, (const float *)A.re, (const float *)A.im, W, mask);
+    else
+        tile_mask_kernel<double><<<grid, 256, 0, s>>>(A.d_meta, A.nd, (const double *)A.re, (const double *)A.im, W,
+                                                      mask);
+    DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
+}
+
+}  // namespace diaq_gb300
