@@ -46,6 +46,10 @@ struct Matrix {
     void *re = nullptr, *im = nullptr;     // device value arrays
     DiagMeta *d_meta = nullptr;            // device copy of meta
     int device = 0;
+    // zero-tile mask of the values (see spmv_kernel.cuh), built on first use by the SpMV entry
+    // points; every function that writes values into an existing matrix clears tmask_ok
+    mutable uint32_t *tmask = nullptr;
+    mutable bool tmask_ok = false;
 
     // bytes per stored value and array (C128F2: a hi and a lo float, in two planes)
     size_t elem() const { return prec == DIAQ_C64 ? sizeof(float) : sizeof(double); }
@@ -86,10 +90,12 @@ int spmv_launch(const Matrix &A, const void *xr, const void *xi, int64_t ldx, vo
                 int64_t ldy, int nrhs, cudaStream_t s);
 
 // Taylor term of the time evolution: term_out = (-i * scale) * (A term_in); acc += term_out
-// (acc = init + term_out when init is given).  Vectors in the matrix's precision.
+// (acc = init + term_out when init is given).  Vectors in the matrix's precision.  tmask: A's
+// zero-tile mask, or NULL.
 int taylor_term_launch(const Matrix &A, const void *tin_r, const void *tin_i, void *tout_r,
                        void *tout_i, void *acc_r, void *acc_i, const void *init_r,
-                       const void *init_i, double scale, int nrhs, int64_t ld, cudaStream_t s);
+                       const void *init_i, double scale, int nrhs, int64_t ld, cudaStream_t s,
+                       const uint32_t *tmask);
 
 int num_sms();
 

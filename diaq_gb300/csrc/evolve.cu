@@ -10,8 +10,9 @@ namespace diaq_gb300 {
 
 // r steps of dt = t / r, each exactly m terms: acc = psi + sum_k term_k with
 // term_k = (-i dt/k) H term_{k-1}, term_0 = psi.  work holds 6 vectors of n doubles.
+// tmask: H's zero-tile mask or NULL.
 int ham_sim_run(const Matrix &H, const double *p0r, const double *p0i, double t, int64_t r, int m,
-                double *outr, double *outi, double *work, cudaStream_t s) {
+                double *outr, double *outi, double *work, cudaStream_t s, const uint32_t *tmask) {
     const int64_t n = H.rows;
     const size_t bytes = sizeof(double) * (size_t)n;
     if (r == 0 || m <= 0) {
@@ -32,7 +33,7 @@ int ham_sim_run(const Matrix &H, const double *p0r, const double *p0i, double t,
         double *tin_r = ar, *tin_i = ai, *tout_r = t0r, *tout_i = t0i;
         for (int k = 1; k <= m; ++k) {
             DQ_TRY(taylor_term_launch(H, tin_r, tin_i, tout_r, tout_i, br, bi, k == 1 ? ar : nullptr,
-                                      k == 1 ? ai : nullptr, dt / (double)k, 1, n, s));
+                                      k == 1 ? ai : nullptr, dt / (double)k, 1, n, s, tmask));
             std::swap(tin_r, tout_r);
             std::swap(tin_i, tout_i);
         }
@@ -62,7 +63,8 @@ int diaq_ham_sim(diaq_matrix_t H, const double *psi0_re, const double *psi0_im, 
     cudaStream_t s = (cudaStream_t)stream;
     double *work = nullptr;
     DQ_CUDA(cudaMallocAsync(&work, sizeof(double) * 6 * (size_t)H->rows, s));
-    const int st = ham_sim_run(*H, psi0_re, psi0_im, t, r, max_iterations, psi_re, psi_im, work, s);
+    const int st = ham_sim_run(*H, psi0_re, psi0_im, t, r, max_iterations, psi_re, psi_im, work, s,
+                               cached_tile_mask(*H, s));
     cudaError_t e = cudaFreeAsync(work, s);
     if (st != DIAQ_OK) return st;
     if (e != cudaSuccess) return cuda_status(e, "cudaFreeAsync", __FILE__, __LINE__);

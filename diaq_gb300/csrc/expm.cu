@@ -154,6 +154,7 @@ __global__ void scale_kernel(T *__restrict__ re, T *__restrict__ im, int64_t n, 
 }
 
 int scale(Matrix &A, int op, double c, cudaStream_t s) {
+    A.tmask_ok = false;
     if (A.capacity == 0) return DIAQ_OK;
     const int grid = (int)std::min<int64_t>((A.capacity + 255) / 256, 8 * num_sms());
     if (A.prec == DIAQ_C128)

@@ -26,7 +26,8 @@
 namespace diaq_gb300 {
 
 int ham_sim_run(const Matrix &H, const double *p0r, const double *p0i, double t, int64_t r, int m,
-                double *outr, double *outi, double *work, cudaStream_t s);
+                double *outr, double *outi, double *work, cudaStream_t s, const uint32_t *tmask);
+const uint32_t *existing_tile_mask(const Matrix &A, cudaStream_t s);
 
 constexpr int64_t kNoAllocMaxRows = int64_t(1) << 16;
 constexpr int kNoAllocVectors = 6;
@@ -74,7 +75,9 @@ int diaq_ham_sim_noalloc(diaq_matrix_t H, const double *psi0_re, const double *p
         return set_error(DIAQ_ERR_INVALID, "hamiltonian_simulation_cuda: vector pointer is NULL");
     double *work = nullptr;
     DQ_TRY(scratch_on_current_device(&work));
-    return ham_sim_run(*H, psi0_re, psi0_im, t, r, max_iterations, psi_re, psi_im, work, (cudaStream_t)stream);
+    // H's zero-tile mask only if an earlier call already built it: building one allocates
+    return ham_sim_run(*H, psi0_re, psi0_im, t, r, max_iterations, psi_re, psi_im, work, (cudaStream_t)stream,
+                       existing_tile_mask(*H, (cudaStream_t)stream));
 }
 
 }  // extern "C"

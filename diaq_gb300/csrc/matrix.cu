@@ -103,6 +103,8 @@ int allocate(Matrix &M, cudaStream_t s) {
     DQ_CUDA(cudaMemsetAsync(M.re, 0, bytes, s));
     DQ_CUDA(cudaMemsetAsync(M.im, 0, bytes, s));
     if (M.nd > 0) {
+        // the zero-tile mask's storage, so that SpMV calls never allocate (it is filled on first use)
+        DQ_CUDA(cudaMalloc(&M.tmask, sizeof(uint32_t) * (size_t)M.nd * (size_t)((M.rows + 1023) / 1024)));
         DQ_CUDA(cudaMalloc(&M.d_meta, sizeof(DiagMeta) * M.nd));
         DQ_CUDA(cudaMemcpyAsync(M.d_meta, M.meta.data(), sizeof(DiagMeta) * M.nd,
                                 cudaMemcpyHostToDevice, s));
@@ -116,8 +118,11 @@ void release(Matrix &M) {
     if (M.re) cudaFree(M.re);
     if (M.im) cudaFree(M.im);
     if (M.d_meta) cudaFree(M.d_meta);
+    if (M.tmask) cudaFree(M.tmask);
     M.re = M.im = nullptr;
     M.d_meta = nullptr;
+    M.tmask = nullptr;
+    M.tmask_ok = false;
 }
 
 int make_zero(int64_t rows, int64_t cols, int32_t nd, const int32_t *off, int prec,
@@ -217,6 +222,7 @@ static dim3 diag_grid(const Matrix &M) {
 }
 
 int scatter_packed(Matrix &M, const double *re, const double *im, cudaStream_t s) {
+    M.tmask_ok = false;
     if (M.nd == 0 || M.total == 0) return DIAQ_OK;
     if (M.prec == DIAQ_C128F2) return f2_scatter(M, re, im, s);
     const dim3 g = diag_grid(M);
@@ -243,6 +249,7 @@ int gather_packed(const Matrix &M, double *re, double *im, cudaStream_t s) {
 // Copy the values of src into dst (dst's offsets are a subset of src's; map[k] = src slot of
 // dst slot k, NULL when the slots coincide).
 static int remap(const Matrix &src, Matrix &dst, const int32_t *d_map, cudaStream_t s) {
+    dst.tmask_ok = false;
     if (dst.nd == 0) return DIAQ_OK;
     const dim3 g = diag_grid(dst);
     if (src.prec == DIAQ_C128 && dst.prec == DIAQ_C128)

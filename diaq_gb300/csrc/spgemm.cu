@@ -256,6 +256,7 @@ int spgemm_numeric(const Matrix &A, const Matrix &B, Matrix &C, cudaStream_t s) 
         return set_error(DIAQ_ERR_INVALID, "diaQMatrix product_cuda: dimension mismatch.");
     if (A.prec != B.prec || A.prec != C.prec)
         return set_error(DIAQ_ERR_INVALID, "product: operands must have the same precision");
+    C.tmask_ok = false;  // new values
     if (C.nd == 0 || C.rows == 0) return DIAQ_OK;
     // dense offset -> slot map of B
     const int64_t bmin = -(B.rows - 1), bmax = B.cols - 1;

@@ -34,7 +34,8 @@ int spmv_launch(const Matrix &A, const void *xr, const void *xi, int64_t ldx, vo
 
 int taylor_term_launch(const Matrix &A, const void *tin_r, const void *tin_i, void *tout_r,
                        void *tout_i, void *acc_r, void *acc_i, const void *init_r,
-                       const void *init_i, double scale, int nrhs, int64_t ld, cudaStream_t s) {
+                       const void *init_i, double scale, int nrhs, int64_t ld, cudaStream_t s,
+                       const uint32_t *tmask) {
     if (A.prec == DIAQ_C128) {
         EpiTaylorRhs<double> e;
         e.tr = (double *)tout_r;
@@ -45,7 +46,8 @@ int taylor_term_launch(const Matrix &A, const void *tin_r, const void *tin_i, vo
         e.initi = (const double *)init_i;
         e.ld = ld;
         e.scale = scale;
-        return launch_dia_spmv_rhs<double>(A, (const double *)tin_r, (const double *)tin_i, ld, nrhs, e, s);
+        return launch_dia_spmv_rhs_cfg<double, EpiTaylorRhs<double>, VecOf<double>::V>(
+            A, (const double *)tin_r, (const double *)tin_i, ld, nrhs, e, s, SpmvCfg{}, tmask);
     }
     EpiTaylorRhs<float> e;
     e.tr = (float *)tout_r;
@@ -56,7 +58,8 @@ int taylor_term_launch(const Matrix &A, const void *tin_r, const void *tin_i, vo
     e.initi = (const float *)init_i;
     e.ld = ld;
     e.scale = (float)scale;
-    return launch_dia_spmv_rhs<float>(A, (const float *)tin_r, (const float *)tin_i, ld, nrhs, e, s);
+    return launch_dia_spmv_rhs_cfg<float, EpiTaylorRhs<float>, VecOf<float>::V>(
+        A, (const float *)tin_r, (const float *)tin_i, ld, nrhs, e, s, SpmvCfg{}, tmask);
 }
 
 }  // namespace diaq_gb300

@@ -110,9 +110,10 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
     f2_spmv_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                    const float *__restrict__ aim, int64_t cap, int64_t rows, const float *__restrict__ xrh,
                    const float *__restrict__ xrl, const float *__restrict__ xih, const float *__restrict__ xil,
-                   double *__restrict__ yr, double *__restrict__ yi) {
+                   double *__restrict__ yr, double *__restrict__ yi, const uint32_t *__restrict__ tmask, int64_t mw) {
     constexpr int V = 4;
     __shared__ DiagMeta sm[kMetaChunk];
+    __shared__ uint32_t smk[kMetaChunk];  // the block's 1024 rows are one mask word
     const int lane = threadIdx.x & 31;
     const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
     const int64_t w0 = r0 - (int64_t)V * lane;
@@ -122,15 +123,20 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, nd - c0);
         __syncthreads();
-        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) sm[i] = meta[c0 + i];
+        for (int i = threadIdx.x; i < cn; i += kSpmvThreads) {
+            sm[i] = meta[c0 + i];
+            smk[i] = tmask ? tmask[(int64_t)(c0 + i) * mw + blockIdx.x] : 0xffffffffu;
+        }
         __syncthreads();
         if (w0 >= rows) continue;
+        const int wbit = (int)((w0 >> 5) & 31);  // the warp's 128 rows: 4 tiles, bits wbit .. wbit + 3
         if (PF > 0 && lane == 0)
             for (int k = 0; k < PF && k < cn; ++k) f2_prefetch_strip(sm[k], w0, are, aim, cap);
         for (int k = 0; k < cn; ++k) {
             if (PF > 0 && lane == 0 && k + PF < cn) f2_prefetch_strip(sm[k + PF], w0, are, aim, cap);
             const int64_t lo = sm[k].lo, hi = sm[k].hi;
-            if (w0 >= hi || w0 + 32 * V <= lo) continue;  // the same for the whole warp
+            // the same for the whole warp (the windows below are shuffled across its lanes)
+            if (w0 >= hi || w0 + 32 * V <= lo || !((smk[k] >> wbit) & 0xfu)) continue;
             const int64_t b = sm[k].base + r0, c = r0 + sm[k].off;
             float arh[V], arl[V], aih[V], ail[V];
             float xrhv[V], xrlv[V], xihv[V], xilv[V];
@@ -211,6 +217,7 @@ static dim3 f2_grid(const Matrix &M) {
 }
 
 int f2_scatter(Matrix &M, const double *re, const double *im, cudaStream_t s) {
+    M.tmask_ok = false;
     if (M.nd == 0) return DIAQ_OK;
     f2_scatter_kernel<<<f2_grid(M), 256, 0, s>>>(M.d_meta, M.nd, re, im, (float *)M.re, (float *)M.im, M.capacity);
     DQ_CUDA(cudaGetLastError());
@@ -227,6 +234,7 @@ int f2_gather(const Matrix &M, double *re, double *im, cudaStream_t s) {
 
 // Same offsets and layout (src and dst planned alike); one precision is C128, the other C128F2.
 int f2_convert(const Matrix &src, Matrix &dst, cudaStream_t s) {
+    dst.tmask_ok = false;
     if (dst.nd == 0) return DIAQ_OK;
     if (src.prec == DIAQ_C128 && dst.prec == DIAQ_C128F2)
         f2_from_c128_kernel<<<f2_grid(dst), 256, 0, s>>>(src.d_meta, src.nd, (const double *)src.re, (const double *)src.im,
@@ -254,7 +262,8 @@ int f2_spmv(const Matrix &A, const double *xr, const double *xi, double *yr, dou
     // 189 us, five or six spill (252, 339 us)
     f2_spmv_kernel<0, 4><<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
                                                                   (const float *)A.im, A.capacity, A.rows, xrh, xrl,
-                                                                  xih, xil, yr, yi);
+                                                                  xih, xil, yr, yi, cached_tile_mask(A, s),
+                                                                  tile_mask_words(A.rows));
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(buf, s);
     if (e != cudaSuccess) return cuda_status(e, "f2 spmv", __FILE__, __LINE__);

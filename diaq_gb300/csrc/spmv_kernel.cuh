@@ -31,6 +31,11 @@ constexpr int kMetaChunk = 256;
 inline int64_t tile_mask_words(int64_t rows) { return (rows + 1023) / 1024; }
 // Fill the mask of A (tile_mask_words(A.rows) * A.nd words) on stream s.
 int build_tile_mask(const Matrix &A, uint32_t *mask, cudaStream_t s);
+// A's own mask, built (and waited for) on first use after its values were last written; NULL when
+// it cannot be had now (s is being captured into a graph, or allocation failed): visit every tile.
+const uint32_t *cached_tile_mask(const Matrix &A, cudaStream_t s);
+// A's mask if it is built and current (never builds, never allocates), else NULL.
+const uint32_t *existing_tile_mask(const Matrix &A, cudaStream_t s);
 
 // VR consecutive values of T as one aligned vector load (VR * sizeof(T) bytes).
 template <typename T, int VR>
@@ -528,7 +533,8 @@ int launch_dia_spmv_pf(const Matrix &A, const float *xr, const float *xi, int64_
 template <typename T, class Epi>
 int launch_dia_spmv_rhs(const Matrix &A, const T *xr, const T *xi, int64_t ldx, int nrhs, Epi epi,
                         cudaStream_t s) {
-    return launch_dia_spmv_rhs_cfg<T, Epi, VecOf<T>::V>(A, xr, xi, ldx, nrhs, epi, s, SpmvCfg{});
+    return launch_dia_spmv_rhs_cfg<T, Epi, VecOf<T>::V>(A, xr, xi, ldx, nrhs, epi, s, SpmvCfg{},
+                                                         cached_tile_mask(A, s));
 }
 
 template <typename T>

@@ -32,17 +32,48 @@ __global__ void tile_mask_kernel(const DiagMeta *__restrict__ meta, int nd, cons
 
 int build_tile_mask(const Matrix &A, uint32_t *mask, cudaStream_t s) {
     if (A.nd == 0 || A.rows == 0) return DIAQ_OK;
-    if (A.prec == DIAQ_C128F2) return set_error(DIAQ_ERR_UNSUPPORTED, "tile mask: c128 or c64 matrices only");
     const int64_t W = tile_mask_words(A.rows);
     if (W > 0x7fffffffll) return set_error(DIAQ_ERR_UNSUPPORTED, "tile mask: too many rows");
     const dim3 grid((unsigned)W, (unsigned)std::min(A.nd, 65535));
-    if (A.prec == DIAQ_C64)
+    // float pairs: the hi planes (the first `capacity` floats); a zero hi part has a zero lo part
+    if (A.prec == DIAQ_C64 || A.prec == DIAQ_C128F2)
         tile_mask_kernel<float><<<grid, 256, 0, s>>>(A.d_meta, A.nd, (const float *)A.re, (const float *)A.im, W, mask);
     else
         tile_mask_kernel<double><<<grid, 256, 0, s>>>(A.d_meta, A.nd, (const double *)A.re, (const double *)A.im, W,
                                                       mask);
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;
+}
+
+const uint32_t *existing_tile_mask(const Matrix &A, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return A.tmask_ok ? A.tmask : nullptr;
+}
+
+const uint32_t *cached_tile_mask(const Matrix &A, cudaStream_t s) {
+    if (A.nd == 0 || A.rows == 0) return nullptr;
+    // no mask in a recorded graph: a replay could outlive the values the mask was taken from
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (A.tmask_ok) return A.tmask;
+    if (!A.tmask && cudaMalloc(&A.tmask, sizeof(uint32_t) * (size_t)A.nd * (size_t)tile_mask_words(A.rows)) != cudaSuccess) {
+        cudaGetLastError();
+        A.tmask = nullptr;
+        return nullptr;
+    }
+    if (build_tile_mask(A, A.tmask, s) != DIAQ_OK || cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    A.tmask_ok = true;
+    return A.tmask;
 }
 
 }  // namespace diaq_gb300

@@ -131,7 +131,9 @@ int diaq_matrix_to_dense(diaq_matrix_t A, double *dense, int on_device, void *st
 
 /* ------------------------------------------------------------------------------------------
  * SpMV.  Replaces spmv_device (src/spMV_gpu.cu:142-168): y = A x on device arrays, y
- * overwritten, asynchronous on stream.
+ * overwritten, asynchronous on stream.  The kernels skip the 32-row tiles of a diagonal that hold
+ * only zeros, from a mask of A taken on the first call after A's values were last written (that
+ * call waits for the stream once); outside graph capture only.
  * ---------------------------------------------------------------------------------------- */
 
 /* c128 matrix, float64 vectors. */

@@ -112,3 +112,51 @@ def test_plain_plan_sees_values_written_after_creation(native):
     Ao = orc.OMatrix(N, N, offA, reA, imA)
     Co = orc.product(Ao, Ao)
     assert maxrel((pr + 1j * pi).cpu().numpy()[0], orc.ham_sim(Co, p, 0.1, 2, 6)) < 1e-12
+
+
+def _spmv(capi, M, x, fn="diaq_spmv_z"):
+    import torch
+
+    dt = torch.float64 if fn == "diaq_spmv_z" else torch.float32
+    xr = torch.from_numpy(x.real.copy()).to("cuda", dt)
+    xi = torch.from_numpy(x.imag.copy()).to("cuda", dt)
+    yr, yi = torch.full_like(xr, float("nan")), torch.full_like(xi, float("nan"))
+    capi.check(getattr(capi.lib(), fn)(M.h, xr.data_ptr(), xi.data_ptr(), yr.data_ptr(), yi.data_ptr(), None))
+    torch.cuda.synchronize()
+    return (yr.double() + 1j * yi.double()).cpu().numpy()
+
+
+@pytest.mark.parametrize("N", [3000, 4096, 33])
+@pytest.mark.parametrize("prec,tol", [(0, 1e-13), (2, 1e-13), (1, 1e-5)])
+def test_spmv_skips_zero_tiles(native, N, prec, tol):
+    capi, _ = native
+    offs = [d for d in [0, 1, -1, 37, -37, 700, -700, 1500, -1500, 64, 5] if abs(d) < N]
+    off, re, im = _zero_tiled(N, offs, 3)
+    M = capi.Matrix.create(N, N, off, re, im, precision=prec)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    want = orc.spmv(orc.OMatrix(N, N, off, re, im), x)
+    fn = "diaq_spmv_c" if prec == 1 else "diaq_spmv_z"
+    for _ in range(2):  # the first call takes the mask, the second uses it
+        assert maxrel(_spmv(capi, M, x, fn), want) < tol
+
+
+def test_spmv_mask_follows_written_values(native):
+    """SpMV of a matrix created as zeros (mask: nothing live), then filled by the numeric SpGEMM:
+    the next SpMV sees the new values."""
+    import ctypes
+
+    capi, _ = native
+    N = 2000
+    offA, reA, imA = _zero_tiled(N, [0, 2, -33, 100], 6)
+    A = capi.Matrix.create(N, N, offA, reA, imA)
+    L = capi.lib()
+    cnt = ctypes.c_int32()
+    offC = np.zeros(len(offA) ** 2, dtype=np.int32)
+    capi.check(L.diaq_spgemm_symbolic(A.h, A.h, offC.ctypes.data, ctypes.byref(cnt), None))
+    C = capi.Matrix.create(N, N, offC[:cnt.value])
+    x = np.random.default_rng(1).standard_normal(N) + 0j
+    assert np.array_equal(_spmv(capi, C, x), np.zeros(N, dtype=complex))
+    capi.check(L.diaq_spgemm_numeric(A.h, A.h, C.h, None))
+    Ao = orc.OMatrix(N, N, offA, reA, imA)
+    assert maxrel(_spmv(capi, C, x), orc.spmv(orc.product(Ao, Ao), x)) < 1e-12
