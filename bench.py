@@ -292,7 +292,8 @@ def run_spmv_only(args):
         w = 8 if name == "c64" else 16
         by = w * live + 2 * w * N
         peak, _ = peaks()
-        out[name] = {"us": us, "gbs": by / us / 1e3, "frac": by / us / 1e3 / peak, "bytes": by}
+        out[name] = {"us": us, "gbs": by / us / 1e3, "frac": by / us / 1e3 / peak, "bytes": by,
+                     "effective_gbs": (w * int(re.size) + 2 * w * N) / us / 1e3}
         if name == "c128":
             out[name]["dfma_per_s"] = 4 * live / (us * 1e-6)
         if name == "c128f2":   # error of the float-pair product against the float64 one
@@ -902,7 +903,9 @@ def run_ours(args, rank, world):
         "spmv_c128": {"us": spmv_us, "gbs": (16 * live + 32 * N) / spmv_us / 1e3,
                       "frac": (16 * live + 32 * N) / spmv_us / 1e3 / peak,
                       "dfma_per_launch": 4 * live, "reps": args.spmv_reps,
-                      "note": "bytes and multiply-adds of the live 32-row tiles (all-zero tiles skipped)"},
+                      "effective_gbs": (16 * total + 32 * N) / spmv_us / 1e3,
+                      "note": "gbs, frac: bytes of the live 32-row tiles (all-zero tiles skipped); effective_gbs: "
+                              "all stored values (w Σlen + 2 w N) per time, the dense-diagonal figure"},
         "spmv_c128f2": {"us": spmv_f2_us, "gbs": (16 * live + 32 * N) / spmv_f2_us / 1e3,
                         "frac": (16 * live + 32 * N) / spmv_f2_us / 1e3 / peak,
                         "maxrel_vs_c128": f2_err, "reps": args.spmv_reps,

@@ -160,3 +160,23 @@ def test_spmv_mask_follows_written_values(native):
     capi.check(L.diaq_spgemm_numeric(A.h, A.h, C.h, None))
     Ao = orc.OMatrix(N, N, offA, reA, imA)
     assert maxrel(_spmv(capi, C, x), orc.spmv(orc.product(Ao, Ao), x)) < 1e-12
+
+
+def test_many_diagonals_cross_the_metadata_chunks(native):
+    """300 diagonals: the kernels stage metadata and mask words in chunks of 256."""
+    capi, _ = native
+    N = 1200
+    offs = sorted(set(range(-150, 150)))
+    off, re, im = _zero_tiled(N, offs, 8)
+    A = orc.OMatrix(N, N, off, re, im)
+    x = np.random.default_rng(5).standard_normal(N) + 1j * np.random.default_rng(6).standard_normal(N)
+    want = orc.spmv(A, x)
+    for prec, fn, tol in ((0, "diaq_spmv_z", 1e-13), (2, "diaq_spmv_z", 1e-13), (1, "diaq_spmv_c", 1e-5)):
+        M = capi.Matrix.create(N, N, off, re, im, precision=prec)
+        assert maxrel(_spmv(capi, M, x, fn), want) < tol, prec
+    re, im = re * 0.05, im * 0.05   # a short step for the evolution
+    for mode, cfg, tol in ((capi.EVOLVE_C128, (4, 2, 0), 1e-12), (capi.EVOLVE_HORNER, (4, 1, 9), 1e-6),
+                           (capi.EVOLVE_MIXED, (4, 1, 6), 1e-6)):
+        Ao, P, got = _run(capi, N, off, re, im, 5, mode, cfg, 0, 8, 2)
+        for q in (0, 4):
+            assert maxrel(got[q], orc.ham_sim(Ao, P[q], 0.1, 2, 8)) < tol, (mode, q)
