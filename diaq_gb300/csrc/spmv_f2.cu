@@ -59,10 +59,33 @@ __global__ void f2_gather_kernel(const DiagMeta *__restrict__ meta, int nd, cons
     }
 }
 
-// float64 vector(s) -> hi/lo planes (n values each; planes of n)
-__global__ void f2_split_vec_kernel(const double *__restrict__ a, float *__restrict__ h, float *__restrict__ l, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        split64(a[i], h[i], l[i]);
+// both float64 vectors of x -> their four hi/lo planes in one launch; vec: x_re and x_im are
+// 16-byte aligned, so pairs of values move as double2 -> float2
+__global__ void f2_split_pair_kernel(const double *__restrict__ xr, const double *__restrict__ xi, int64_t n, int vec,
+                                     float *__restrict__ rh, float *__restrict__ rl, float *__restrict__ ih,
+                                     float *__restrict__ il) {
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t n2 = n / 2;
+        for (int64_t i = t0; i < n2; i += stride) {
+            const double2 a = reinterpret_cast<const double2 *>(xr)[i], b = reinterpret_cast<const double2 *>(xi)[i];
+            float h0, l0, h1, l1;
+            split64(a.x, h0, l0);
+            split64(a.y, h1, l1);
+            reinterpret_cast<float2 *>(rh)[i] = make_float2(h0, h1);
+            reinterpret_cast<float2 *>(rl)[i] = make_float2(l0, l1);
+            split64(b.x, h0, l0);
+            split64(b.y, h1, l1);
+            reinterpret_cast<float2 *>(ih)[i] = make_float2(h0, h1);
+            reinterpret_cast<float2 *>(il)[i] = make_float2(l0, l1);
+        }
+        done = 2 * n2;
+    }
+    for (int64_t i = done + t0; i < n; i += stride) {
+        split64(xr[i], rh[i], rl[i]);
+        split64(xi[i], ih[i], il[i]);
+    }
 }
 
 struct F2 {
@@ -141,6 +164,8 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
             float arh[V], arl[V], aih[V], ail[V];
             float xrhv[V], xrlv[V], xihv[V], xilv[V];
             if (w0 >= lo && w0 + 32 * V <= hi) {
+                // an aligned window needs no shuffle: a lane whose tile is zero drops out alone
+                if ((sm[k].off & 3) == 0 && !((smk[k] >> ((r0 >> 5) & 31)) & 1u)) continue;
                 load_vec_stream<float, V>(arh, are + b);
                 load_vec_stream<float, V>(arl, are + cap + b);
                 load_vec_stream<float, V>(aih, aim + b);
@@ -256,8 +281,8 @@ int f2_spmv(const Matrix &A, const double *xr, const double *xi, double *yr, dou
     DQ_CUDA(cudaMallocAsync(&buf, sizeof(float) * 4 * (size_t)std::max<int64_t>(np, 32), s));
     float *xrh = buf, *xrl = buf + np, *xih = buf + 2 * np, *xil = buf + 3 * np;
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * num_sms()));
-    f2_split_vec_kernel<<<g, 256, 0, s>>>(xr, xrh, xrl, n);
-    f2_split_vec_kernel<<<g, 256, 0, s>>>(xi, xih, xil, n);
+    const int vec = ((uintptr_t)xr % 16 == 0) && ((uintptr_t)xi % 16 == 0);
+    f2_split_pair_kernel<<<g, 256, 0, s>>>(xr, xi, n, vec, xrh, xrl, xih, xil);
     // four blocks per SM (64 registers): 166.8 us on the 20-qubit chain; three (80 registers)
     // 189 us, five or six spill (252, 339 us)
     f2_spmv_kernel<0, 4><<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
