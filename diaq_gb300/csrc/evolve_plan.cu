@@ -34,6 +34,7 @@
 
 #include "spmv_il.cuh"
 #include "spmv_pipe.cuh"
+#include "spmv_tma.cuh"
 
 namespace diaq_gb300 {
 
@@ -384,6 +385,9 @@ struct EvolvePlan {
     bool renorm = false;  // rescale every state to norm 1 (float64) after each step
     double *part = nullptr;  // renormalisation partial sums, nrhs * kNormBlocks
     uint32_t *tmask = nullptr;  // zero-tile mask of the matrix the term kernels read (Hc, or H for C128)
+    int *err = nullptr;           // bounded waits of the bulk-copy kernel (variant 10) record here
+    int *err_host = nullptr;      // pinned copy of *err taken after each run
+    cudaEvent_t err_ev = nullptr; // ... and the event that says it has landed
     int sp = 4;           // interleaved layout: nrhs rounded up to a power of two >= 4 (<= 32 used)
     int64_t n_pad = 0;    // rows rounded up to a multiple of 32
 
@@ -397,6 +401,9 @@ struct EvolvePlan {
         if (buf) cudaFree(buf);
         if (part) cudaFree(part);
         if (tmask) cudaFree(tmask);
+        if (err) cudaFree(err);
+        if (err_host) cudaFreeHost(err_host);
+        if (err_ev) cudaEventDestroy(err_ev);
         if (Hc) destroy(Hc);
         if (s) cudaStreamDestroy(s);
     }
@@ -409,12 +416,39 @@ struct diaq_evolve_s : public diaq_gb300::EvolvePlan {};
 
 namespace diaq_gb300 {
 
-// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8) or 9 (8
-// states per thread; 4 when the padded state count is 4).
+// The interleaved kernel for plan variant 6 (no ring), 7 (ring of 4), 8 (ring of 8), 9 (8
+// states per thread; 4 when the padded state count is 4) or 10 (bulk copies through shared
+// memory, spmv_tma.cuh; 8 or 4 states per thread as 9; the register kernel of 9 when the matrix
+// has more diagonals than one metadata chunk).
 template <class Epi>
 int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &e) {
     const int v = P.cfg.pipe;
-    const bool eight = v == 9 && P.sp % 8 == 0;
+    const bool eight = v >= 9 && P.sp % 8 == 0;
+    if ((v == 10 || v == 11) && P.Hc->nd <= kMetaChunk) {
+        const int G = P.sp % 8 == 0 ? 8 : 4;
+        const int R = 32 * (8 / (P.sp / G));
+        const unsigned gt = (unsigned)((P.n_pad + R - 1) / R);
+        const bool win = v == 10;
+        const size_t smem = tma_smem_bytes(R, P.sp, win, win ? 4 : 8);
+        const float *are = (const float *)P.Hc->re, *aim = (const float *)P.Hc->im;
+        const int64_t mw = tile_mask_words(P.n);
+        const DiagMeta *md = P.Hc->d_meta;
+        const int nd = P.Hc->nd;
+        if (G == 8 && win)
+            dia_spmv_tma_kernel<Epi, 8, true, 4><<<gt, kTmaThreads, smem, P.s>>>(md, nd, are, aim, P.n, P.n_pad, xr, xi,
+                                                                                 P.tmask, mw, e, P.err);
+        else if (G == 8)
+            dia_spmv_tma_kernel<Epi, 8, false, 8><<<gt, kTmaThreads, smem, P.s>>>(md, nd, are, aim, P.n, P.n_pad, xr, xi,
+                                                                                  P.tmask, mw, e, P.err);
+        else if (win)
+            dia_spmv_tma_kernel<Epi, 4, true, 4><<<gt, kTmaThreads, smem, P.s>>>(md, nd, are, aim, P.n, P.n_pad, xr, xi,
+                                                                                 P.tmask, mw, e, P.err);
+        else
+            dia_spmv_tma_kernel<Epi, 4, false, 8><<<gt, kTmaThreads, smem, P.s>>>(md, nd, are, aim, P.n, P.n_pad, xr, xi,
+                                                                                  P.tmask, mw, e, P.err);
+        DQ_CUDA(cudaGetLastError());
+        return DIAQ_OK;
+    }
     const int groups = P.sp / (eight ? 8 : 4);          // warps per row block of 32: 1, 2, 4 or 8
     const int64_t rows_per_block = 32 * (8 / groups);
     const unsigned g = (unsigned)((P.n_pad + rows_per_block - 1) / rows_per_block);
@@ -432,6 +466,16 @@ int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &
     else
         dia_spmv_il_kernel<Epi, 0><<<g, kSpmvThreads, 0, P.s>>>(md, nd, are, aim, P.n, xr, xi, tm, mw, e);
     DQ_CUDA(cudaGetLastError());
+    return DIAQ_OK;
+}
+
+// The bulk-copy kernels hold up to kTmaStages stages of 25 KB of dynamic shared memory: raise
+// their limit once, before any launch is recorded.
+template <class Epi>
+static int allow_tma_smem() {
+    const int b = 128 * 1024;
+    DQ_CUDA(cudaFuncSetAttribute(dia_spmv_tma_kernel<Epi, 8, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    DQ_CUDA(cudaFuncSetAttribute(dia_spmv_tma_kernel<Epi, 4, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     return DIAQ_OK;
 }
 
@@ -459,6 +503,16 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     if (e == cudaSuccess && bytes) e = cudaMalloc(&P->buf, bytes);
     if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
     if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
+    if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128)
+        st = mode == DIAQ_EVOLVE_HORNER ? allow_tma_smem<EpiHornerIL>() : allow_tma_smem<EpiMixedIL>();
+    if (st == DIAQ_OK) {
+        e = cudaMalloc(&P->err, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemsetAsync(P->err, 0, sizeof(int), P->s);
+        if (e == cudaSuccess) e = cudaMallocHost(&P->err_host, sizeof(int));
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->err_ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) *P->err_host = 0;
+        if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
+    }
     if (st == DIAQ_OK && H.nd > 0) {
         // the mask of the plan's own c64 copy is built once; that of the caller's c128 matrix
         // again at every run (its values may have changed)
@@ -721,7 +775,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
                 {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
                 {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
-                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}};
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}, {4, 1, 10}, {4, 1, 11}};
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -803,6 +857,9 @@ static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt
     if (steps < 0 || m < 0 || sl < 0 || sl > 20) return set_error(DIAQ_ERR_INVALID, "evolve: bad steps / s / m");
     if (!pr || !pi) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
     if (steps == 0 || m == 0 || P.n == 0) return DIAQ_OK;
+    // an earlier run's bulk-copy kernel gave up a wait (the copy of its flag has landed)
+    if (cudaEventQuery(P.err_ev) == cudaSuccess && *P.err_host != 0)
+        return set_error(DIAQ_ERR_CUDA, "evolve: the bulk-copy term kernel timed out waiting on a shared-memory stage");
     if (!P.Hc && P.tmask) DQ_TRY(build_tile_mask(*P.H, P.tmask, user));
     DQ_TRY(ensure_renorm_buffer(P));
     if (!P.tuned) DQ_TRY(autotune(P, dt, sl, m, pr, pi, ld, user));
@@ -829,6 +886,8 @@ static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt
     // everything below runs on the caller's stream
     if (P.f32()) DQ_TRY(fp32_state(P, pr, pi, user));  // fp32(psi) for the first sub-step
     for (int64_t i = 0; i < steps; ++i) DQ_CUDA(cudaGraphLaunch(it->second, user));
+    DQ_CUDA(cudaMemcpyAsync(P.err_host, P.err, sizeof(int), cudaMemcpyDeviceToHost, user));
+    DQ_CUDA(cudaEventRecord(P.err_ev, user));
     return DIAQ_OK;
 }
 
@@ -869,9 +928,9 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
         const bool vr_ok = rows_per_thread == 1 || rows_per_thread == 2 || (f32 && rows_per_thread == 4);
         if (states_per_block < 1 || states_per_block > 8 || !vr_ok)
             return set_error(DIAQ_ERR_INVALID, "evolve: states_per_block in 1..8, rows_per_thread 1, 2 (or 4 for mixed)");
-        if (pipelined < 0 || pipelined > 9 || pipelined == 5)
+        if (pipelined < 0 || pipelined > 11 || pipelined == 5)
             return set_error(DIAQ_ERR_INVALID, "evolve: pipelined is 0 (registers), 1 (cp.async), 2 or 3 (L2 prefetch), "
-                                               "4 (shuffled windows), 6-9 (interleaved states)");
+                                               "4 (shuffled windows), 6-11 (interleaved states)");
         if (pipelined >= 6) {
             if (!(f32 && states_per_block == 4 && rows_per_thread == 1))
                 return set_error(DIAQ_ERR_INVALID, "evolve: the interleaved kernel is the mixed mode's, 4 states and "
