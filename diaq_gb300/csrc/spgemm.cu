@@ -191,13 +191,22 @@ __global__ void spgemm_pairs_kernel(const DiagMeta *__restrict__ mA, int ndA, co
     }
 }
 
-// Block (x, y): row tile x of the C diagonals y, y + gridDim.y, ...; thread t owns V rows.
+// bit of row r's 32-row tile in diagonal slot j of a zero-tile mask (mw words per diagonal)
+__device__ __forceinline__ bool tile_live(const uint32_t *__restrict__ mask, int64_t mw, int j, int64_t r) {
+    return (__ldg(mask + (int64_t)j * mw + (r >> 10)) >> ((r >> 5) & 31)) & 1u;
+}
+
+// Block (x, y): row tile x of the C diagonals y, y + gridDim.y, ...; thread t owns V rows.  With
+// the operands' zero-tile masks (maskA, maskB) a pair is skipped where A's tile or both B tiles
+// that its rows read are zero: a product with a zero factor adds nothing.
 template <typename T>
 __global__ void __launch_bounds__(kSpmvThreads)
     spgemm_numeric_kernel(const DiagMeta *__restrict__ mA, const T *__restrict__ Are, const T *__restrict__ Aim,
                           const DiagMeta *__restrict__ mB, const T *__restrict__ Bre, const T *__restrict__ Bim,
                           const DiagMeta *__restrict__ mC, int ndC, const int64_t *__restrict__ pstart,
-                          const int2 *__restrict__ pairs, T *__restrict__ Cre, T *__restrict__ Cim) {
+                          const int2 *__restrict__ pairs, T *__restrict__ Cre, T *__restrict__ Cim,
+                          const uint32_t *__restrict__ maskA, int64_t mwA, const uint32_t *__restrict__ maskB,
+                          int64_t mwB) {
     constexpr int V = VecOf<T>::V;
     const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
     for (int c = blockIdx.y; c < ndC; c += gridDim.y) {
@@ -213,6 +222,11 @@ __global__ void __launch_bounds__(kSpmvThreads)
             int64_t lo, hi;
             pair_rows(ma, mb, mc, lo, hi);
             if (r0 + V <= lo || r0 >= hi) continue;
+            if (maskA) {  // r0 .. r0 + V - 1 share one tile (V | 32); their B rows span at most two
+                if (!tile_live(maskA, mwA, ab.x, r0)) continue;
+                const int64_t b0 = max(r0, lo) + ma.off, b1 = min(r0 + V, hi) - 1 + ma.off;
+                if (!tile_live(maskB, mwB, ab.y, b0) && !tile_live(maskB, mwB, ab.y, b1)) continue;
+            }
             T ar[V], ai[V], br[V], bi[V];
             load_vec<T, V>(ar, Are + ma.base + r0);
             load_vec<T, V>(ai, Aim + ma.base + r0);
@@ -298,14 +312,18 @@ int spgemm_numeric(const Matrix &A, const Matrix &B, Matrix &C, cudaStream_t s) 
         const int V = A.prec == DIAQ_C128 ? 2 : 4;
         // up to 64 C diagonals per block row: each block walks several diagonals' pairs
         const dim3 grid(spmv_blocks(maxrows, V), (unsigned)std::min<int64_t>(C.nd, 64));
+        // the operands' masks (both or neither); taken here, outside any graph capture
+        const uint32_t *ka = cached_tile_mask(A, s), *kb = ka ? cached_tile_mask(B, s) : nullptr;
+        if (!kb) ka = nullptr;
+        const int64_t wa = tile_mask_words(A.rows), wb = tile_mask_words(B.rows);
         if (A.prec == DIAQ_C128)
             spgemm_numeric_kernel<double><<<grid, kSpmvThreads, 0, s>>>(
                 A.d_meta, (const double *)A.re, (const double *)A.im, B.d_meta, (const double *)B.re,
-                (const double *)B.im, C.d_meta, C.nd, dstart, dpairs, (double *)C.re, (double *)C.im);
+                (const double *)B.im, C.d_meta, C.nd, dstart, dpairs, (double *)C.re, (double *)C.im, ka, wa, kb, wb);
         else
             spgemm_numeric_kernel<float><<<grid, kSpmvThreads, 0, s>>>(
                 A.d_meta, (const float *)A.re, (const float *)A.im, B.d_meta, (const float *)B.re,
-                (const float *)B.im, C.d_meta, C.nd, dstart, dpairs, (float *)C.re, (float *)C.im);
+                (const float *)B.im, C.d_meta, C.nd, dstart, dpairs, (float *)C.re, (float *)C.im, ka, wa, kb, wb);
         e = cudaGetLastError();
     }
     // the host vectors must outlive the async copies
