@@ -4,7 +4,7 @@ The network (FP32 MLP 16 -> 64 -> 64 -> 21 + 30, kernels in csrc/mlp.cu) maps 16
 of (H, t, tol) to logits over s in 0..20 and m in 1..30.  Every proposal is checked a posteriori
 before use; the plain norm-bound selection (diaq_select_sm: the reference's scaling rule
 s = ceil(log2(t ||H||_1)) with the Taylor remainder bound for m) is both the fallback and the
-judge of the gain.
+yardstick of the gain.
 
 Chain.  For a probe state psi (unit, seeded) one device run of M = 60 products gives
 u_k = (-i H)^k psi / k!, k = 0..M.  For a sub-step tau the k-th Taylor term of exp(-i tau H) psi
