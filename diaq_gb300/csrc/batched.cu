@@ -603,7 +603,7 @@ static int autotune(Batch &B) {
     }
     const std::string key = batch_key(B);
     int k = 0, v = 0;
-    // a cached shape is used only if this build can launch it
+    // a cached shape is used only if the compiled kernels include it
     if (cache_lookup(key, k, v) && (k == 1 || k == 2 || k == 4 || k == 8) &&
         (v == 1 || v == 2 || (B.prec == DIAQ_C64 && v == 4))) {
         B.cfg = SpmvCfg{k, v};

@@ -788,7 +788,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     const std::string key = tune_key(P, sl, m);
     auto cache = read_cache();
     auto hit = cache.find(key);
-    // a cached shape is used only if it is still one of this build's candidates
+    // a cached shape is used only if it is still one of the library's candidates
     const bool known = hit != cache.end() && std::any_of(cand.begin(), cand.end(), [&](const SpmvCfg &c) {
                            return c.kmax == hit->second.kmax && c.vr == hit->second.vr && c.pipe == hit->second.pipe;
                        });

@@ -32,7 +32,7 @@ typedef enum {
     DIAQ_ERR_INVALID = 1,     /* bad argument: shapes, offsets, null pointers */
     DIAQ_ERR_CUDA = 2,        /* a CUDA runtime call failed */
     DIAQ_ERR_OOM = 3,         /* device allocation failed */
-    DIAQ_ERR_UNSUPPORTED = 4, /* valid request this build does not handle */
+    DIAQ_ERR_UNSUPPORTED = 4, /* valid request the library does not handle */
     DIAQ_ERR_TIMEOUT = 5      /* a bounded device-side wait gave up */
 } diaq_status;
 
