@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // One item of an interleaved instance: row block `tile` (32 * 8 / (sp / G) rows) and all sp
 // states.  Phases as in batched_phase_kernel; the initialisation and copy phases move the item's
 // rows of every state, which are one contiguous range of the tiled vectors.
-template <int G>
+template <int G, bool HORNER>
 __device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm, uint32_t *smk, int64_t tile,
                                                 int phase) {
     const int quads = I.sp >> 2, groups = I.sp / G;
@@ -295,7 +295,7 @@ __device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm
     const bool first = (k == 1), last = (k == I.m);
     const float *xr, *xi;
     float *outr, *outi;
-    if (I.horner) {
+    if (HORNER) {
         xr = first ? var : ((k - 1) & 1) ? vbr : (float *)I.hr;
         xi = first ? vai : ((k - 1) & 1) ? vbi : (float *)I.hi;
         outr = (k & 1) ? vbr : (float *)I.hr;
@@ -331,7 +331,7 @@ __device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm
         }
     }
     if (r >= I.rows) return;
-    if (I.horner) {  // the last step reads w_1, not fp32(psi): refreshing v_a there is safe
+    if constexpr (HORNER) {  // the last step reads w_1, not fp32(psi): refreshing v_a there is safe
         const EpiHornerIL e{outr, outi, var, vai, var, vai, I.pr, I.pi, ld, I.sp, I.nrhs,
                             (float)(I.tau / (double)(I.m - k + 1)), last};
 #pragma unroll
@@ -352,10 +352,13 @@ __device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm
     }
 }
 
-// Items of the instances with G states per thread (separate lists and launches for G = 8 and 4,
-// so that each kernel keeps only its own registers).
-template <int G>
-__global__ void __launch_bounds__(kSpmvThreads, 4)
+// Items of the instances with G states per thread in the Horner (HORNER) or the compensated form
+// (separate lists and launches, so that each kernel keeps only its own registers).  Blocks per
+// SM, measured on the 512-instance set: Horner at six (7,040 states x steps/s; 6,751 at five,
+// 5,904 at four, 5,543 at eight, whose spills cost more than the occupancy gains), the
+// compensated form at five (5,759; 5,637 at six).
+template <int G, bool HORNER>
+__global__ void __launch_bounds__(kSpmvThreads, HORNER ? 6 : 5)
     batched_il_kernel(const BatchInst *__restrict__ insts, const BatchItem *__restrict__ items, int phase) {
     __shared__ DiagMeta sm[kMetaChunk];
     __shared__ uint32_t smk[kMetaChunk];
@@ -363,7 +366,7 @@ __global__ void __launch_bounds__(kSpmvThreads, 4)
     const BatchItem item = items[blockIdx.x];
     if (threadIdx.x == 0) si = insts[item.inst];
     __syncthreads();
-    batched_il_item<G>(si, sm, smk, item.tile, phase);
+    batched_il_item<G, HORNER>(si, sm, smk, item.tile, phase);
 }
 
 struct Batch {
@@ -373,8 +376,10 @@ struct Batch {
     BatchInst *d_inst = nullptr;
     BatchItem *d_items = nullptr;     // planar instances
     int n_items = 0;
-    BatchItem *d_il_items = nullptr;  // interleaved instances, one block each: G = 8 first, then G = 4
-    int n_il_items = 0, n_il8 = 0;
+    BatchItem *d_il_items = nullptr;  // interleaved instances, one block each, in four segments:
+    int n_il_items = 0;               // (G 8, Horner), (G 8, compensated), (G 4, Horner), (G 4, compensated)
+    int il_seg[5] = {0, 0, 0, 0, 0};  // segment starts
+    std::vector<char> items_horner;   // Horner flags the lists were built for
     bool il_on = true;                // interleave the instances that can be
     int items_il = -1;                // il_on of the current item lists
     void *work = nullptr;
@@ -412,20 +417,23 @@ static int vr_of(const Batch &B) { return B.cfg.vr > 0 ? B.cfg.vr : (B.prec == D
 // Item list for the current launch shape: largest instances first.
 static int build_items(Batch &B) {
     const int K = B.cfg.kmax, VR = vr_of(B);
-    if (B.d_items && B.items_cfg_k == K && B.items_cfg_vr == VR && B.items_il == (int)B.il_on) return DIAQ_OK;
+    std::vector<char> hf(B.inst.size());
+    for (size_t i = 0; i < hf.size(); ++i) hf[i] = (char)B.inst[i].horner;
+    if (B.d_items && B.items_cfg_k == K && B.items_cfg_vr == VR && B.items_il == (int)B.il_on && hf == B.items_horner)
+        return DIAQ_OK;
     std::vector<int> order(B.inst.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         return B.inst[a].rows * B.inst[a].nd * B.inst[a].nrhs > B.inst[b].rows * B.inst[b].nd * B.inst[b].nrhs;
     });
-    std::vector<BatchItem> items, il_items, il4_items;
+    std::vector<BatchItem> items, seg[4];
     for (int i : order) {
         const BatchInst &I = B.inst[i];
         if (I.il) {
             const bool eight = I.sp % 8 == 0;
             const int64_t rpb = 32 * (8 / (I.sp / (eight ? 8 : 4)));
-            for (int64_t t = 0; t < (I.rows + rpb - 1) / rpb; ++t)
-                (eight ? il_items : il4_items).push_back(BatchItem{i, (int)t, 0, 0});
+            std::vector<BatchItem> &dst = seg[(eight ? 0 : 2) + (I.horner ? 0 : 1)];
+            for (int64_t t = 0; t < (I.rows + rpb - 1) / rpb; ++t) dst.push_back(BatchItem{i, (int)t, 0, 0});
             continue;
         }
         const int64_t tiles = (B.inst[i].rows + (int64_t)kSpmvThreads * VR - 1) / ((int64_t)kSpmvThreads * VR);
@@ -433,8 +441,12 @@ static int build_items(Batch &B) {
         for (int64_t t = 0; t < tiles; ++t)
             for (int c = 0; c < chunks; ++c) items.push_back(BatchItem{i, (int)t, c, 0});
     }
-    B.n_il8 = (int)il_items.size();
-    il_items.insert(il_items.end(), il4_items.begin(), il4_items.end());
+    std::vector<BatchItem> il_items;
+    for (int q = 0; q < 4; ++q) {
+        B.il_seg[q] = (int)il_items.size();
+        il_items.insert(il_items.end(), seg[q].begin(), seg[q].end());
+    }
+    B.il_seg[4] = (int)il_items.size();
     if (B.d_items) cudaFree(B.d_items);
     if (B.d_il_items) cudaFree(B.d_il_items);
     B.d_items = B.d_il_items = nullptr;
@@ -447,6 +459,7 @@ static int build_items(Batch &B) {
     B.items_cfg_k = K;
     B.items_cfg_vr = VR;
     B.items_il = (int)B.il_on;
+    B.items_horner = hf;
     return DIAQ_OK;
 }
 
@@ -487,9 +500,12 @@ static int launch_phase(const Batch &B, int phase, cudaStream_t s) {
 
 static int phase(const Batch &B, int p, cudaStream_t s) {
     DQ_TRY(B.prec == DIAQ_C64 ? launch_phase<float>(B, p, s) : launch_phase<double>(B, p, s));
-    if (B.n_il8 > 0) batched_il_kernel<8><<<B.n_il8, kSpmvThreads, 0, s>>>(B.d_inst, B.d_il_items, p);
-    if (B.n_il_items > B.n_il8)
-        batched_il_kernel<4><<<B.n_il_items - B.n_il8, kSpmvThreads, 0, s>>>(B.d_inst, B.d_il_items + B.n_il8, p);
+    const BatchItem *it = B.d_il_items;
+    const int *q = B.il_seg;
+    if (q[1] > q[0]) batched_il_kernel<8, true><<<q[1] - q[0], kSpmvThreads, 0, s>>>(B.d_inst, it + q[0], p);
+    if (q[2] > q[1]) batched_il_kernel<8, false><<<q[2] - q[1], kSpmvThreads, 0, s>>>(B.d_inst, it + q[1], p);
+    if (q[3] > q[2]) batched_il_kernel<4, true><<<q[3] - q[2], kSpmvThreads, 0, s>>>(B.d_inst, it + q[2], p);
+    if (q[4] > q[3]) batched_il_kernel<4, false><<<q[4] - q[3], kSpmvThreads, 0, s>>>(B.d_inst, it + q[3], p);
     DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;
 }
