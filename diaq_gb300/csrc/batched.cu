@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // states.  Phases as in batched_phase_kernel; the initialisation and copy phases move the item's
 // rows of every state, which are one contiguous range of the tiled vectors.
 template <int G, bool HORNER>
-__device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm, uint32_t *smk, int64_t tile,
+__device__ __forceinline__ void batched_il_item(const BatchInst &I, int4 *sq, int64_t *sb, int64_t tile,
                                                 int phase) {
     const int quads = I.sp >> 2, groups = I.sp / G;
     const int64_t rpb = 32 * (8 / groups);
@@ -317,18 +317,14 @@ __device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm
         const int cn = min(kMetaChunk, I.nd - c0);
         __syncthreads();
         for (int j = threadIdx.x; j < cn; j += kSpmvThreads) {
-            sm[j] = I.meta[c0 + j];
-            smk[j] = I.tmask[(int64_t)(c0 + j) * I.mw + (r0 >> 10)];  // the item's <= 256 rows: one word
+            const DiagMeta m = I.meta[c0 + j];
+            // the item's <= 256 rows: one mask word
+            sq[j] = make_int4(m.off, (int)m.lo, (int)m.hi, (int)I.tmask[(int64_t)(c0 + j) * I.mw + (r0 >> 10)]);
+            sb[j] = m.base;
         }
         __syncthreads();
         if (r >= I.rows) continue;
-        const int tbit = (int)((r >> 5) & 31);
-#pragma unroll 4
-        for (int j = 0; j < cn; ++j) {
-            if (r < sm[j].lo || r >= sm[j].hi || !((smk[j] >> tbit) & 1u)) continue;
-            il_term<G>(r + sm[j].off, g * (G / 4), quads, __ldcs(are + sm[j].base + r), __ldcs(aim + sm[j].base + r), xr,
-                       xi, accr, acci);
-        }
+        il_accumulate32<G>(sq, sb, cn, (int)r, g * (G / 4), quads, are, aim, xr, xi, accr, acci);
     }
     if (r >= I.rows) return;
     if constexpr (HORNER) {  // the last step reads w_1, not fp32(psi): refreshing v_a there is safe
@@ -356,17 +352,18 @@ __device__ __forceinline__ void batched_il_item(const BatchInst &I, DiagMeta *sm
 // (separate lists and launches, so that each kernel keeps only its own registers).  Blocks per
 // SM, measured on the 512-instance set: Horner at six (7,040 states x steps/s; 6,751 at five,
 // 5,904 at four, 5,543 at eight, whose spills cost more than the occupancy gains), the
-// compensated form at five (5,759; 5,637 at six).
+// compensated form at five (5,759; 5,637 at six); with the compact metadata loop
+// (il_accumulate32) 7,571 and 6,091.
 template <int G, bool HORNER>
 __global__ void __launch_bounds__(kSpmvThreads, HORNER ? 6 : 5)
     batched_il_kernel(const BatchInst *__restrict__ insts, const BatchItem *__restrict__ items, int phase) {
-    __shared__ DiagMeta sm[kMetaChunk];
-    __shared__ uint32_t smk[kMetaChunk];
+    __shared__ int4 sq[kMetaChunk];
+    __shared__ int64_t sb[kMetaChunk];
     __shared__ BatchInst si;
     const BatchItem item = items[blockIdx.x];
     if (threadIdx.x == 0) si = insts[item.inst];
     __syncthreads();
-    batched_il_item<G, HORNER>(si, sm, smk, item.tile, phase);
+    batched_il_item<G, HORNER>(si, sq, sb, item.tile, phase);
 }
 
 struct Batch {
@@ -706,7 +703,8 @@ int diaq_batch_create(int n_inst, const diaq_matrix_t *H, const int *nrhs, doubl
         sp = 4;
         while (sp < nrhs[i]) sp *= 2;
         n_pad = (H[i]->rows + 31) / 32 * 32;
-        return prec == DIAQ_C64 && nrhs[i] >= 4 && nrhs[i] <= 32;
+        // (the interleaved kernels index rows and tiled vectors in 32 bits)
+        return prec == DIAQ_C64 && nrhs[i] >= 4 && nrhs[i] <= 32 && (int64_t)sp * n_pad < ((int64_t)1 << 31);
     };
     auto vec_bytes = [&](int i) {
         int sp;

@@ -178,4 +178,32 @@ __device__ __forceinline__ void il_term(int64_t c, int g0, int quads, float a, f
     il_fma<G>(a, b, w, accr, acci);
 }
 
+// The diagonals k < cn of one metadata chunk for row r (32-bit row and window arithmetic: rows
+// and n_pad * sp below 2^31).  sq[k] = (offset, lo, hi, mask word of the block's rows), sb[k] =
+// value base: one 16-byte and one 8-byte shared-memory load per diagonal; a warp skips a dead
+// tile or a diagonal outside its rows together.
+template <int G>
+__device__ __forceinline__ void il_accumulate32(const int4 *sq, const int64_t *sb, int cn, int r, int g0, int quads,
+                                                const float *__restrict__ are, const float *__restrict__ aim,
+                                                const float *__restrict__ xr, const float *__restrict__ xi,
+                                                float (&accr)[G], float (&acci)[G]) {
+    const int tbit = (r >> 5) & 31;
+#pragma unroll 4
+    for (int k = 0; k < cn; ++k) {
+        const int4 q = sq[k];
+        if (r < q.y || r >= q.z || !(((uint32_t)q.w >> tbit) & 1u)) continue;
+        const int64_t vb = sb[k] + r;
+        const float a = __ldcs(are + vb), b = __ldcs(aim + vb);
+        const int c = r + q.x;
+        IlWindow<G> w;
+#pragma unroll
+        for (int h = 0; h < G / 4; ++h) {
+            const int at = ((((c >> 5) * quads) + g0 + h) << 7) + ((c & 31) << 2);
+            w.x[h] = __ldg(reinterpret_cast<const float4 *>(xr + at));
+            w.y[h] = __ldg(reinterpret_cast<const float4 *>(xi + at));
+        }
+        il_fma<G>(a, b, w, accr, acci);
+    }
+}
+
 }  // namespace diaq_gb300

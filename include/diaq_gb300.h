@@ -261,7 +261,8 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
  * interleaved in tiles of 32 rows x 4 states (any window one aligned vector per lane) and load the
  * matrix 0 / 4 / 8 diagonals ahead into registers; 9 with 8 states per thread; 10 / 11 feed the
  * block's live diagonals through a ring of shared-memory stages filled by bulk asynchronous copies
- * (matrix values and state windows / matrix values only).  Every kernel of a
+ * (matrix values and state windows / matrix values only); 12 is 9 with 32-bit row arithmetic and
+ * each diagonal's metadata in one 16-byte shared-memory record (n_pad * states < 2^31).  Every kernel of a
  * plan skips the 32-row tiles of a diagonal that hold only zeros (a mask built from the matrix the
  * plan reads).
  * 0 states = choose automatically: on the first run the autotuner times the candidate shapes on

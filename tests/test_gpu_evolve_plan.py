@@ -146,7 +146,7 @@ def test_prefetch_kernel_edges(native, n, variant):
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
 
 
-@pytest.mark.parametrize("variant", [6, 7, 9, 10, 11])
+@pytest.mark.parametrize("variant", [6, 7, 9, 10, 11, 12])
 @pytest.mark.parametrize("k,sl,m,renorm", [(5, 0, 11, False), (5, 1, 7, True), (8, 0, 12, False), (3, 2, 5, True),
                                             (12, 0, 9, False), (20, 1, 6, True)])
 def test_interleaved_states(native, k, sl, m, renorm, variant):
@@ -170,7 +170,7 @@ def test_interleaved_states(native, k, sl, m, renorm, variant):
 
 
 @pytest.mark.parametrize("cfg", [(8, 4, 0), (2, 4, 0), (4, 2, 0), (8, 1, 0), (4, 1, 6), (4, 1, 8), (4, 1, 9), (4, 1, 10),
-                                 (4, 1, 11)])
+                                 (4, 1, 11), (4, 1, 12)])
 @pytest.mark.parametrize("sl,m", [(0, 12), (1, 7), (0, 1)])
 def test_horner_accuracy(native, cfg, sl, m):
     """Horner-form float32 evaluation: within 1e-6 of the FP64 oracle after 20 steps, every

@@ -67,7 +67,7 @@ def test_plain_skips_zero_tiles(native, N, cfg):
 
 @pytest.mark.parametrize("k", [3, 5, 16, 32])
 @pytest.mark.parametrize("cfg", [(8, 4, 0), (8, 2, 0), (4, 1, 6), (4, 1, 7), (4, 1, 8), (4, 1, 9), (4, 1, 10),
-                                 (4, 1, 11)])
+                                 (4, 1, 11), (4, 1, 12)])
 @pytest.mark.parametrize("mode", ["mixed", "horner"])
 def test_float_forms_skip_zero_tiles(native, k, cfg, mode):
     capi, _ = native
@@ -178,7 +178,8 @@ def test_many_diagonals_cross_the_metadata_chunks(native):
         assert maxrel(_spmv(capi, M, x, fn), want) < tol, prec
     re, im = re * 0.05, im * 0.05   # a short step for the evolution
     for mode, cfg, tol in ((capi.EVOLVE_C128, (4, 2, 0), 1e-12), (capi.EVOLVE_HORNER, (4, 1, 9), 1e-6),
-                           (capi.EVOLVE_MIXED, (4, 1, 6), 1e-6), (capi.EVOLVE_HORNER, (4, 1, 10), 1e-6)):
+                           (capi.EVOLVE_MIXED, (4, 1, 6), 1e-6), (capi.EVOLVE_HORNER, (4, 1, 10), 1e-6),
+                           (capi.EVOLVE_HORNER, (4, 1, 12), 1e-6)):
         Ao, P, got = _run(capi, N, off, re, im, 5, mode, cfg, 0, 8, 2)
         for q in (0, 4):
             assert maxrel(got[q], orc.ham_sim(Ao, P[q], 0.1, 2, 8)) < tol, (mode, q)
