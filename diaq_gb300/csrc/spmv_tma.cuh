@@ -13,7 +13,9 @@
 // global memory.
 //
 // Every wait is bounded: after kTmaSpinLimit polls the waiting warp records an error in *err and
-// leaves; the plan reports the error on its next run.
+// leaves -- the producer only after waiting (bounded again) for the copies it has in flight, so
+// that no copy lands in the shared memory of a finished block; the plan reports the error on its
+// next run.
 #pragma once
 
 #include "spmv_il.cuh"
@@ -123,7 +125,11 @@ __global__ void __launch_bounds__(kTmaThreads)
         for (int j = 0; j < nd; ++j) {
             if (!(smk[j] & bmask)) continue;
             const int s = i % S;
-            if (i >= S && !mbar_wait_bounded(&empty[s], (uint32_t)((i / S - 1) & 1), err, 1)) return;
+            if (i >= S && !mbar_wait_bounded(&empty[s], (uint32_t)((i / S - 1) & 1), err, 1)) {
+                for (int f = i - S; f < i; ++f)  // the last fill of every stage
+                    mbar_wait_bounded(&full[f % S], (uint32_t)((f / S) & 1), err, 3);
+                return;
+            }
             const DiagMeta m = sm[j];
             float *st = stages + s * SF;
             // matrix rows [a0, a0 + R) clipped to the diagonal's stored rows widened to 16-byte
