@@ -133,3 +133,26 @@ def test_batched_interleaved_matches_planar_and_oracle(native, horner):
             want = orc.ham_sim(A, P0[i][q], 0.06, 3, m[i], substeps=1 << s[i])
             err = np.linalg.norm(out[True][i][q] - want) / np.linalg.norm(want)
             assert err < 1e-6, (i, q, err)
+
+
+def test_batched_layout_toggle_on_one_batch(native):
+    """set_interleaved between runs of the same batch re-records the step with the other item
+    lists; the results agree with a batch that never switched."""
+    import torch
+
+    capi, _ = native
+    s, m = [0, 1, 0, 0, 1, 0, 0, 2, 0], [9, 7, 12, 6, 5, 11, 8, 3, 10]
+    mats, oms, prs, pis, P0 = _make(capi, IL_SPECS, 1)
+    B = capi.Batch(mats, prs, pis)
+    B.set_horner(True)
+    B.run(0.02, s, m, 2)
+    B.set_interleaved(False)
+    B.run(0.02, s, m, 1)
+    B.set_interleaved(True)
+    B.run(0.02, s, m, 1)
+    torch.cuda.synchronize()
+    for i, A in enumerate(oms):
+        got = (prs[i] + 1j * pis[i]).cpu().numpy()
+        for q in range(P0[i].shape[0]):
+            want = orc.ham_sim(A, P0[i][q], 0.08, 4, m[i], substeps=1 << s[i])
+            assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, (i, q)

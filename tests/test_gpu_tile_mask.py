@@ -183,3 +183,39 @@ def test_many_diagonals_cross_the_metadata_chunks(native):
         Ao, P, got = _run(capi, N, off, re, im, 5, mode, cfg, 0, 8, 2)
         for q in (0, 4):
             assert maxrel(got[q], orc.ham_sim(Ao, P[q], 0.1, 2, 8)) < tol, (mode, q)
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (1, 1e-5)])
+def test_spgemm_skips_zero_tiles(native, prec, tol):
+    """A B with zero tiles in both factors and odd offsets (a thread's B rows straddle two tiles):
+    the same offsets as the oracle, values within tol; rectangular shapes."""
+    import ctypes
+
+    capi, _ = native
+
+    def rand(rows, cols, offs, seed):
+        r = np.random.default_rng(seed)
+        re, im = [], []
+        for d in offs:
+            lo, hi = max(0, -d), min(rows, cols - d)
+            L = hi - lo
+            rr = lo + np.arange(L)
+            a = r.standard_normal(L) + 1j * r.standard_normal(L)
+            dead = r.random((rows + 31) // 32) < 0.5
+            a[dead[rr // 32]] = 0
+            re.append(a.real)
+            im.append(a.imag)
+        return orc.OMatrix(rows, cols, np.array(offs, dtype=np.int32), np.concatenate(re), np.concatenate(im))
+
+    A = rand(1500, 1300, [0, 1, -3, 33, -65, 7, 200], 1)
+    B = rand(1300, 1700, [0, -1, 5, 31, -40, 129, 3], 2)
+    dA = capi.Matrix.create(A.rows, A.cols, A.off, A.re, A.im, precision=prec)
+    dB = capi.Matrix.create(B.rows, B.cols, B.off, B.re, B.im, precision=prec)
+    out = ctypes.c_void_p()
+    capi.check(capi.lib().diaq_spgemm(dA.h, dB.h, 0, None, ctypes.byref(out)))
+    C = capi.Matrix(out)
+    off, re, im = C.download()
+    want = orc.product(A, B, prune_result=False)
+    assert np.array_equal(np.sort(off), np.sort(want.off))
+    got = orc.OMatrix(A.rows, B.cols, off, re, im)
+    assert maxrel(got.to_dense(), want.to_dense()) < tol
