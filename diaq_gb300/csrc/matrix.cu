@@ -56,6 +56,9 @@ int64_t diag_len(int64_t rows, int64_t cols, int64_t d) {
 
 int plan_layout(Matrix &M, int64_t rows, int64_t cols, int32_t nd, const int32_t *off) {
     if (rows < 0 || cols < 0) return set_error(DIAQ_ERR_INVALID, "matrix shape must be non-negative");
+    // the kernels keep row indices, offsets and row ranges in 32 bits (the reference's are 32-bit too)
+    if (rows >= ((int64_t)1 << 31) || cols >= ((int64_t)1 << 31))
+        return set_error(DIAQ_ERR_UNSUPPORTED, "matrix dimensions must be below 2^31");
     if (nd < 0) return set_error(DIAQ_ERR_INVALID, "diagonal count must be non-negative");
     if (nd > 0 && !off) return set_error(DIAQ_ERR_INVALID, "offsets pointer is NULL");
     M.rows = rows;

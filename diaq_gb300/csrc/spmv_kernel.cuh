@@ -114,8 +114,10 @@ __global__ void __launch_bounds__(kSpmvThreads)
                     int64_t mw, Epi epi0) {
     constexpr int V = VR;
     constexpr int VB = VR * (int)sizeof(T);
-    __shared__ DiagMeta sm[kMetaChunk];
-    __shared__ uint32_t smk[kMetaChunk];  // zero-tile mask word of the block rows, per diagonal
+    // per diagonal: offset, row range and the zero-tile mask word of the block's rows in one
+    // 16-byte record (rows < 2^31), the value base beside it
+    __shared__ int4 sq[kMetaChunk];
+    __shared__ int64_t sb[kMetaChunk];
     const int chunk = (int)(blockIdx.x % (unsigned)nchunk);
     const int64_t tile = blockIdx.x / (unsigned)nchunk;
     const int q0 = chunk * K;
@@ -137,17 +139,20 @@ __global__ void __launch_bounds__(kSpmvThreads)
         const int cn = min(kMetaChunk, nd - c0);
         __syncthreads();
         for (int i = threadIdx.x; i < cn; i += kSpmvThreads) {
-            sm[i] = meta[c0 + i];
-            smk[i] = tmask ? tmask[(int64_t)(c0 + i) * mw + mword] : 0xffffffffu;
+            const DiagMeta m = meta[c0 + i];
+            const uint32_t w = tmask ? tmask[(int64_t)(c0 + i) * mw + mword] : 0xffffffffu;
+            sq[i] = make_int4(m.off, (int)m.lo, (int)m.hi, (int)w);
+            sb[i] = m.base;
         }
         __syncthreads();
         if (r0 >= rows) continue;
 #pragma unroll 2
         for (int k = 0; k < cn; ++k) {
-            const int64_t lo = sm[k].lo, hi = sm[k].hi;
-            if (r0 + V <= lo || r0 >= hi || !((smk[k] >> tbit) & 1u)) continue;
-            const int64_t base = sm[k].base;
-            const int64_t d = sm[k].off;
+            const int4 q = sq[k];
+            const int64_t lo = q.y, hi = q.z;
+            if (r0 + V <= lo || r0 >= hi || !(((uint32_t)q.w >> tbit) & 1u)) continue;
+            const int64_t base = sb[k];
+            const int64_t d = q.x;
             T ar[V], ai[V];
             load_vec_stream<T, V>(ar, are + base + r0);
             load_vec_stream<T, V>(ai, aim + base + r0);
