@@ -59,3 +59,9 @@ def test_invalid_arguments_fail_without_a_gpu(lib):
     assert st == 1 and b"offsets" in L.diaq_last_error()
     assert L.diaq_spmv_z(None, None, None, None, None, None) == 1
     assert L.diaq_matrix_destroy(None) == 0
+    import numpy as np
+
+    off = np.zeros(1, dtype=np.int32)
+    st = L.diaq_matrix_create(1 << 31, 1 << 31, 1, off.ctypes.data, None, None, 0, 0, None, ctypes.byref(out))
+    assert st == 4 and b"below 2^31" in L.diaq_last_error()   # 32-bit row indices in the kernels
+    assert L.diaq_batch_set_interleaved(None, 1) == 1
