@@ -111,32 +111,20 @@ __device__ __forceinline__ void f2_mac(F2 &s, float ah, float al, float xh, floa
 // every matrix load is a 16-byte vector of 4 rows.  Strips that lie inside a diagonal read the
 // four x planes as aligned vectors shifted across lanes (the x planes are this file's scratch,
 // padded to a multiple of 32 values, so the aligned vectors stay inside them; values past column
-// cols are read but never used).  PF > 0 also prefetches the warp's 128-row strip of the four
-// matrix planes into L2 PF diagonals ahead; on the 20-qubit XXZ chain that measured slower
-// (216 vs 194 us), so the entry point runs PF = 0.
+// cols are read but never used).  Each diagonal's offset, row range and the block's mask word are
+// staged as one 16-byte shared-memory record.  (Prefetching the warp's strip of the four matrix
+// planes into L2 a few diagonals ahead measured slower on the 20-qubit XXZ chain, 216 against
+// 194 us, and was dropped.)
 
-__device__ __forceinline__ void f2_prefetch_strip(const DiagMeta &m, int64_t w0, const float *are,
-                                                  const float *aim, int64_t cap) {
-    const int64_t a = w0 > (m.lo & ~int64_t(31)) ? w0 : (m.lo & ~int64_t(31));
-    const int64_t hi32 = (m.hi + 31) & ~int64_t(31);
-    const int64_t b = (w0 + 128) < hi32 ? (w0 + 128) : hi32;
-    if (a >= b) return;
-    const unsigned bytes = (unsigned)(b - a) * 4u;
-    prefetch_l2_bulk(are + m.base + a, bytes);
-    prefetch_l2_bulk(are + cap + m.base + a, bytes);
-    prefetch_l2_bulk(aim + m.base + a, bytes);
-    prefetch_l2_bulk(aim + cap + m.base + a, bytes);
-}
-
-template <int PF, int MINB>
+template <int MINB>
 __global__ void __launch_bounds__(kSpmvThreads, MINB)
     f2_spmv_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                    const float *__restrict__ aim, int64_t cap, int64_t rows, const float *__restrict__ xrh,
                    const float *__restrict__ xrl, const float *__restrict__ xih, const float *__restrict__ xil,
                    double *__restrict__ yr, double *__restrict__ yi, const uint32_t *__restrict__ tmask, int64_t mw) {
     constexpr int V = 4;
-    __shared__ DiagMeta sm[kMetaChunk];
-    __shared__ uint32_t smk[kMetaChunk];  // the block's 1024 rows are one mask word
+    __shared__ int4 sq[kMetaChunk];     // offset, lo, hi, mask word (the block's 1024 rows are one word)
+    __shared__ int64_t sb[kMetaChunk];  // value base
     const int lane = threadIdx.x & 31;
     const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
     const int64_t w0 = r0 - (int64_t)V * lane;
@@ -147,25 +135,26 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
         const int cn = min(kMetaChunk, nd - c0);
         __syncthreads();
         for (int i = threadIdx.x; i < cn; i += kSpmvThreads) {
-            sm[i] = meta[c0 + i];
-            smk[i] = tmask ? tmask[(int64_t)(c0 + i) * mw + blockIdx.x] : 0xffffffffu;
+            const DiagMeta m = meta[c0 + i];
+            const uint32_t w = tmask ? tmask[(int64_t)(c0 + i) * mw + blockIdx.x] : 0xffffffffu;
+            sq[i] = make_int4(m.off, (int)m.lo, (int)m.hi, (int)w);
+            sb[i] = m.base;
         }
         __syncthreads();
         if (w0 >= rows) continue;
         const int wbit = (int)((w0 >> 5) & 31);  // the warp's 128 rows: 4 tiles, bits wbit .. wbit + 3
-        if (PF > 0 && lane == 0)
-            for (int k = 0; k < PF && k < cn; ++k) f2_prefetch_strip(sm[k], w0, are, aim, cap);
         for (int k = 0; k < cn; ++k) {
-            if (PF > 0 && lane == 0 && k + PF < cn) f2_prefetch_strip(sm[k + PF], w0, are, aim, cap);
-            const int64_t lo = sm[k].lo, hi = sm[k].hi;
+            const int4 q = sq[k];
+            const int64_t lo = q.y, hi = q.z;
+            const uint32_t mword = (uint32_t)q.w;
             // the same for the whole warp (the windows below are shuffled across its lanes)
-            if (w0 >= hi || w0 + 32 * V <= lo || !((smk[k] >> wbit) & 0xfu)) continue;
-            const int64_t b = sm[k].base + r0, c = r0 + sm[k].off;
+            if (w0 >= hi || w0 + 32 * V <= lo || !((mword >> wbit) & 0xfu)) continue;
+            const int64_t b = sb[k] + r0, c = r0 + q.x;
             float arh[V], arl[V], aih[V], ail[V];
             float xrhv[V], xrlv[V], xihv[V], xilv[V];
             if (w0 >= lo && w0 + 32 * V <= hi) {
                 // an aligned window needs no shuffle: a lane whose tile is zero drops out alone
-                if ((sm[k].off & 3) == 0 && !((smk[k] >> ((r0 >> 5) & 31)) & 1u)) continue;
+                if ((q.x & 3) == 0 && !((mword >> ((r0 >> 5) & 31)) & 1u)) continue;
                 load_vec_stream<float, V>(arh, are + b);
                 load_vec_stream<float, V>(arl, are + cap + b);
                 load_vec_stream<float, V>(aih, aim + b);
@@ -285,7 +274,7 @@ int f2_spmv(const Matrix &A, const double *xr, const double *xi, double *yr, dou
     f2_split_pair_kernel<<<g, 256, 0, s>>>(xr, xi, n, vec, xrh, xrl, xih, xil);
     // four blocks per SM (64 registers): 166.8 us on the 20-qubit chain; three (80 registers)
     // 189 us, five or six spill (252, 339 us)
-    f2_spmv_kernel<0, 4><<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
+    f2_spmv_kernel<4><<<spmv_blocks(A.rows, 4), kSpmvThreads, 0, s>>>(A.d_meta, A.nd, (const float *)A.re,
                                                                   (const float *)A.im, A.capacity, A.rows, xrh, xrl,
                                                                   xih, xil, yr, yi, cached_tile_mask(A, s),
                                                                   tile_mask_words(A.rows));
