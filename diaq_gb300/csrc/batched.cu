@@ -81,8 +81,8 @@ template <typename T, int K, int VR>
 __global__ void __launch_bounds__(kSpmvThreads)
     batched_phase_kernel(const BatchInst *__restrict__ insts, const BatchItem *__restrict__ items, int n_items,
                          int phase) {
-    __shared__ DiagMeta sm[kMetaChunk];
-    __shared__ uint32_t smk[kMetaChunk];
+    __shared__ int4 sq[kMetaChunk];     // offset, lo, hi, mask word of the item's rows
+    __shared__ int64_t sb[kMetaChunk];  // value base
     __shared__ BatchInst si;
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
         const BatchItem item = items[it];
@@ -144,16 +144,18 @@ __global__ void __launch_bounds__(kSpmvThreads)
             // the item's 256 VR rows (VR | 4) lie in one 1024-row mask word, a thread's VR in one tile
             const int64_t mword = ((int64_t)item.tile * kSpmvThreads * VR) >> 10;
             for (int j = threadIdx.x; j < cn; j += kSpmvThreads) {
-                sm[j] = I.meta[c0 + j];
-                smk[j] = I.tmask[(int64_t)(c0 + j) * I.mw + mword];
+                const DiagMeta m = I.meta[c0 + j];
+                sq[j] = make_int4(m.off, (int)m.lo, (int)m.hi, (int)I.tmask[(int64_t)(c0 + j) * I.mw + mword]);
+                sb[j] = m.base;
             }
             __syncthreads();
             if (r0 >= I.rows) continue;
             const int tbit = (int)((r0 >> 5) & 31);
             for (int j = 0; j < cn; ++j) {
-                const int64_t lo = sm[j].lo, hi = sm[j].hi;
-                if (r0 + VR <= lo || r0 >= hi || !((smk[j] >> tbit) & 1u)) continue;
-                const int64_t base = sm[j].base, c = r0 + sm[j].off;
+                const int4 q = sq[j];
+                const int64_t lo = q.y, hi = q.z;
+                if (r0 + VR <= lo || r0 >= hi || !(((uint32_t)q.w >> tbit) & 1u)) continue;
+                const int64_t base = sb[j], c = r0 + q.x;
                 T ar[VR], ai[VR];
                 load_vec_stream<T, VR>(ar, are + base + r0);
                 load_vec_stream<T, VR>(ai, aim + base + r0);
