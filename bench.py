@@ -507,18 +507,30 @@ def _ops_xxz(args, out, L, peak, peak_kind, dfma_peak, cpu, gpu_wall, cpu_wall):
     torch.cuda.empty_cache()
     algo_bytes = 16 * (2 * int(re.size) + sum_c) + 4 * len(off) * len(off)
     Ho = orc.OMatrix(N, N, off, re, im)
-    c_prod20, _ = cpu_wall(lambda: cpu.product(Ho, Ho))
+    c_prod20, Wc = cpu_wall(lambda: cpu.product(Ho, Ho))
+    # parity at full size: the pruned product's offsets bit-exact, its Frobenius norm (both sides
+    # over every stored value) relative
+    Cp = ctypes.c_void_p()
+    capi.check(L.diaq_spgemm(H.h, H.h, 1, None, ctypes.byref(Cp)))
+    Cp = capi.Matrix(Cp)
+    fro = ctypes.c_double()
+    capi.check(L.diaq_frobenius(Cp.h, ctypes.byref(fro), None))
+    offs_equal = bool(np.array_equal(Cp.offsets(), np.asarray(Wc.off)))
+    fro_cpu = float(np.sqrt(np.sum(np.asarray(Wc.re) ** 2) + np.sum(np.asarray(Wc.im) ** 2)))
+    del Cp, Wc
+    torch.cuda.empty_cache()
     out[f"xxz{args.n}"] = {
         "product_HH": {"gpu_ms": 1e3 * t_full, "symbolic_ms": 1e3 * t_sym, "cpu_ms": 1e3 * c_prod20,
                        "result_offsets": int(cnt.value), "result_stored_values": int(sum_c),
+                       "offsets_equal_cpu": offs_equal, "frobenius_rel_diff_cpu": abs(fro.value - fro_cpu) / fro_cpu,
                        "complex_macs": int(macs), "complex_macs_live_tiles": int(live_macs),
                        "algorithmic_bytes": int(algo_bytes),
                        "gbs": algo_bytes / t_full / 1e9, "frac_hbm": algo_bytes / t_full / 1e9 / peak,
                        "dfma_per_s": 4 * live_macs / t_full, "frac_fp64": 4 * live_macs / t_full / dfma_peak,
-                       "note": "includes the device allocation of C and the dry-run; c128 numeric is "
-                               "bound by FP64 issue (4 DFMA per complex multiply-add); products with a "
-                               "factor in an all-zero 32-row tile are skipped, so the FP64 rate counts "
-                               "complex_macs_live_tiles"}}
+                       "note": "includes the device allocation and zeroing of C and the dry-run; products "
+                               "with a factor in an all-zero 32-row tile are skipped, so the FP64 rate counts "
+                               "complex_macs_live_tiles (4 DFMA each); parity: the pruned product's offsets "
+                               "and Frobenius norm against the CPU product"}}
     out["peak_hbm_gbs"] = peak
     out["peak_kind"] = peak_kind
     print(json.dumps(out), flush=True)
