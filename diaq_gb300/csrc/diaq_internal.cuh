@@ -73,13 +73,18 @@ int cuda_status(cudaError_t e, const char *what, const char *file, int line);
 int64_t diag_len(int64_t rows, int64_t cols, int64_t d);
 // Lay out a matrix of these offsets (fills meta, capacity, total); validates the offsets.
 int plan_layout(Matrix &M, int64_t rows, int64_t cols, int32_t nd, const int32_t *off);
-// Allocate zeroed device storage for a planned matrix and upload its metadata.
-int allocate(Matrix &M, cudaStream_t s);
+// Allocate device storage for a planned matrix (zeroed unless zero == false) and upload its
+// metadata.
+int allocate(Matrix &M, cudaStream_t s, bool zero = true);
 void release(Matrix &M);
 
-// A new matrix with these offsets, all values zero.
+// A new matrix with these offsets, all values zero; zero == false leaves the storage
+// uninitialised for a caller that writes every stored value and then calls zero_gaps.
 int make_zero(int64_t rows, int64_t cols, int32_t nd, const int32_t *off, int prec,
-              cudaStream_t s, Matrix **out);
+              cudaStream_t s, Matrix **out, bool zero = true);
+// Zero what lies outside the stored rows: the guard before the first diagonal, the alignment gaps
+// between diagonals and the tail of the allocation (every plane).
+int zero_gaps(const Matrix &M, cudaStream_t s);
 
 // Packed (reference layout) float64 values <-> device layout.
 int scatter_packed(Matrix &M, const double *re, const double *im, cudaStream_t s);

@@ -98,13 +98,15 @@ int plan_layout(Matrix &M, int64_t rows, int64_t cols, int32_t nd, const int32_t
     return DIAQ_OK;
 }
 
-int allocate(Matrix &M, cudaStream_t s) {
+int allocate(Matrix &M, cudaStream_t s, bool zero) {
     cudaGetDevice(&M.device);
     const size_t bytes = (size_t)M.capacity * M.elem();
     DQ_CUDA(cudaMalloc(&M.re, bytes));
     DQ_CUDA(cudaMalloc(&M.im, bytes));
-    DQ_CUDA(cudaMemsetAsync(M.re, 0, bytes, s));
-    DQ_CUDA(cudaMemsetAsync(M.im, 0, bytes, s));
+    if (zero) {
+        DQ_CUDA(cudaMemsetAsync(M.re, 0, bytes, s));
+        DQ_CUDA(cudaMemsetAsync(M.im, 0, bytes, s));
+    }
     if (M.nd > 0) {
         // the zero-tile mask's storage, so that SpMV calls never allocate (it is filled on first use)
         DQ_CUDA(cudaMalloc(&M.tmask, sizeof(uint32_t) * (size_t)M.nd * (size_t)((M.rows + 1023) / 1024)));
@@ -129,18 +131,43 @@ void release(Matrix &M) {
 }
 
 int make_zero(int64_t rows, int64_t cols, int32_t nd, const int32_t *off, int prec,
-              cudaStream_t s, Matrix **out) {
+              cudaStream_t s, Matrix **out, bool zero) {
     if (prec != DIAQ_C128 && prec != DIAQ_C64 && prec != DIAQ_C128F2)
         return set_error(DIAQ_ERR_INVALID, "precision must be DIAQ_C128, DIAQ_C64 or DIAQ_C128F2");
     Matrix *M = new diaq_matrix_s();
     M->prec = prec;
     int st = plan_layout(*M, rows, cols, nd, off);
-    if (st == DIAQ_OK) st = allocate(*M, s);
+    if (st == DIAQ_OK) st = allocate(*M, s, zero);
     if (st != DIAQ_OK) {
         destroy(M);
         return st;
     }
     *out = M;
+    return DIAQ_OK;
+}
+
+// Block j zeroes gap j: [0, start of diagonal 0) for j = 0, [end of j - 1, start of j) between
+// diagonals, [end of the last, capacity) for j = nd -- in each of the `planes` planes of
+// `capacity` elements of size esz in re and im.
+__global__ void zero_gaps_kernel(const DiagMeta *__restrict__ meta, int nd, int64_t capacity, int esz, int planes,
+                                 unsigned char *re, unsigned char *im) {
+    const int j = blockIdx.x;
+    const int64_t a = j == 0 ? 0 : meta[j - 1].base + meta[j - 1].hi;
+    const int64_t b = j == nd ? capacity : meta[j].base + meta[j].lo;
+    for (int p = 0; p < planes; ++p)
+        for (int64_t e = a + threadIdx.x; e < b; e += blockDim.x)
+            for (int k = 0; k < esz; ++k) {
+                re[(p * capacity + e) * esz + k] = 0;
+                im[(p * capacity + e) * esz + k] = 0;
+            }
+}
+
+int zero_gaps(const Matrix &M, cudaStream_t s) {
+    const int planes = M.prec == DIAQ_C128F2 ? 2 : 1;
+    const int esz = M.prec == DIAQ_C128 ? 8 : 4;
+    zero_gaps_kernel<<<M.nd + 1, 64, 0, s>>>(M.d_meta, M.nd, M.capacity, esz, planes, (unsigned char *)M.re,
+                                             (unsigned char *)M.im);
+    DQ_CUDA(cudaGetLastError());
     return DIAQ_OK;
 }
 

@@ -341,8 +341,10 @@ int spgemm(const Matrix &A, const Matrix &B, bool prune, cudaStream_t s, Matrix 
     std::vector<int32_t> offC;
     DQ_TRY(spgemm_symbolic(A, B, offC, s));
     Matrix *C = nullptr;
-    DQ_TRY(make_zero(A.rows, B.cols, (int32_t)offC.size(), offC.data(), A.prec, s, &C));
+    // the numeric pass writes every stored value of C: only the gaps around them need zeroing
+    DQ_TRY(make_zero(A.rows, B.cols, (int32_t)offC.size(), offC.data(), A.prec, s, &C, false));
     int st = spgemm_numeric(A, B, *C, s);
+    if (st == DIAQ_OK) st = zero_gaps(*C, s);
     if (st == DIAQ_OK && prune) {
         Matrix *P = nullptr;
         st = prune_matrix(*C, s, &P);
