@@ -253,3 +253,39 @@ def test_pipelined_large_unaligned_offsets(native):
     for q in (0, 4):
         want = orc.ham_sim(A, P[q], 0.1, 2, 10)
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6
+
+
+@pytest.mark.parametrize("model", ["xxz", "tfim"])
+@pytest.mark.parametrize("mode", ["horner", "mixed"])
+def test_full_size_chosen_form_against_c128(native, mode, model):
+    """The bench line's workload size: a 20-qubit chain (XXZ, periodic; transverse-field Ising,
+    open), 8 states, 5 steps of dt = 0.05 in the float32 forms on the bench line's kernel
+    (variant 12, zero tiles skipped), against the complex128 plan at a tight step tolerance --
+    within the 1e-6 bar."""
+    import ctypes
+
+    capi, _ = native
+    N, off, re, im = ham.xxz(20) if model == "xxz" else ham.tfim(20)
+    H = capi.Matrix.create(N, N, off, re, im)
+    nrm = ctypes.c_double()
+    capi.check(capi.lib().diaq_norm1_est(H.h, ctypes.byref(nrm), None))
+    s_c, m_c = capi.select_sm(nrm.value, 0.05, 1e-8, 1.0, 100)
+    s_r, m_r = capi.select_sm(nrm.value, 0.05, 1e-14, 1.0, 100)
+    P = ham.random_state(N, 0, k=8)
+    out = {}
+    for name, md, sl, m, cfg in (("c128", capi.EVOLVE_C128, s_r, m_r, None),
+                                 (mode, capi.EVOLVE_HORNER if mode == "horner" else capi.EVOLVE_MIXED, s_c, m_c,
+                                  (4, 1, 12))):
+        import torch
+
+        E = capi.Evolve(H, 8, md)
+        if cfg:
+            E.set_config(*cfg)
+        pr = torch.from_numpy(np.ascontiguousarray(P.real)).cuda()
+        pi = torch.from_numpy(np.ascontiguousarray(P.imag)).cuda()
+        E.run(pr, pi, N, 0.05, 5, sl, m)
+        out[name] = _result(pr, pi)
+        del E
+    for q in range(8):
+        want = out["c128"][q]
+        assert np.linalg.norm(out[mode][q] - want) / np.linalg.norm(want) < 1e-6, q
