@@ -20,6 +20,14 @@
 // have used):
 //   C128:  psi (caller's), sum, term_a, term_b                 (float64)
 //   MIXED: psi (caller's, float64); v_a, v_b, hi, lo           (float32)
+//
+// Term kernels (the launch shape's `pipe` variant; the autotuner times the candidates once per
+// plan shape and caches its choice): 0 the planar register kernel of spmv_kernel.cuh; 1-4 its
+// float pipelines (cp.async, L2 prefetch, shuffled windows); 6-9 and 12 the states interleaved
+// in 32-row tiles (spmv_il.cuh: 4 or 8 states per thread, an optional register ring of matrix
+// values, 12 with compact 32-bit metadata -- the fastest on the 20-qubit chain); 10-11 the same
+// fed through shared memory by bulk asynchronous copies (spmv_tma.cuh).  Every kernel skips the
+// 32-row tiles of a diagonal that hold only zeros (the plan's zero-tile mask).
 #include <sys/stat.h>
 
 #include <algorithm>
