@@ -29,6 +29,7 @@
 // once per row block for all the states.  The other instances (1-3 or more than 32 states,
 // complex128) keep the planar layout and the persistent kernel above.
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
@@ -581,11 +582,13 @@ static void cache_store(const std::string &key, int k, int v) {
         for (size_t k2 = 1; k2 <= dir.size(); ++k2)
             if (k2 == dir.size() || dir[k2] == '/') mkdir(dir.substr(0, k2).c_str(), 0755);
     }
-    std::ofstream f(path + ".tmp");
+    // a temporary of this process's own, renamed into place: ranks sharing HOME never interleave
+    const std::string tmp = path + "." + std::to_string((long)getpid()) + ".tmp";
+    std::ofstream f(tmp);
     if (!f) return;
     f << out;
     f.close();
-    std::rename((path + ".tmp").c_str(), path.c_str());
+    std::rename(tmp.c_str(), path.c_str());
 }
 
 static std::string batch_key(const Batch &B) {

@@ -29,6 +29,7 @@
 // fed through shared memory by bulk asynchronous copies (spmv_tma.cuh).  Every kernel skips the
 // 32-row tiles of a diagonal that hold only zeros (the plan's zero-tile mask).
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
@@ -809,7 +810,9 @@ static void write_cache(const std::map<std::string, SpmvCfg> &c) {
         for (size_t k = 1; k <= dir.size(); ++k)
             if (k == dir.size() || dir[k] == '/') mkdir(dir.substr(0, k).c_str(), 0755);
     }
-    std::ofstream f(path + ".tmp");
+    // a temporary of this process's own, renamed into place: ranks sharing HOME never interleave
+    const std::string tmp = path + "." + std::to_string((long)getpid()) + ".tmp";
+    std::ofstream f(tmp);
     if (!f) return;
     f << "{\n";
     size_t n = 0;
@@ -818,7 +821,7 @@ static void write_cache(const std::map<std::string, SpmvCfg> &c) {
           << (++n < c.size() ? ",\n" : "\n");
     f << "}\n";
     f.close();
-    std::rename((path + ".tmp").c_str(), path.c_str());
+    std::rename(tmp.c_str(), path.c_str());
 }
 
 static std::string tune_key(const EvolvePlan &P, int sl, int m) {
