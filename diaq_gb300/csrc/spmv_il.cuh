@@ -20,13 +20,14 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// Index of the float4 holding states 4 quad .. 4 quad + 3 of row r in the tiled interleaved layout
-// (quads = sp / 4).
+// Float index of state 4 quad of row r in the tiled interleaved layout (quads = sp / 4); states
+// 4 quad .. 4 quad + 3 of the row follow it as one 16-byte-aligned float4.
 __device__ __forceinline__ int64_t il_at(int64_t r, int quad, int quads) {
     return ((r >> 5) * quads + quad) * 128 + ((r & 31) << 2);
 }
 
-// One Taylor term's epilogue for four interleaved states of one row; the arithmetic of EpiMixed.
+// One Taylor term's epilogue for four interleaved states of one row: the compensated forward sum
+// (the arithmetic of the planar EpiMixed of the evolution plans).
 struct EpiMixedIL {
     float *vr, *vi;                 // term out (interleaved)
     float *hr, *hi_, *lr, *li;      // compensated sum (interleaved)
