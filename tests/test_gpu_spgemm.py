@@ -126,3 +126,27 @@ def _randm(rng, r, c, nd):
     offs = rng.choice(np.arange(-(r - 1), c), size=min(nd, r + c - 1), replace=False)
     tot = sum(orc.diag_len(r, c, int(d)) for d in offs)
     return orc.OMatrix(r, c, offs, rng.standard_normal(tot), rng.standard_normal(tot))
+
+
+def test_full_size_xxz20_square_structure_and_norm(native):
+    """Config 2's H H at full size (20 qubits: 731 result diagonals, 689 M stored values): the
+    pruned offsets bit-exact and the Frobenius norm within 1e-12 of the oracle's product's -- the
+    size-independent checks (the values themselves are checked at smaller sizes above)."""
+    import ctypes
+
+    capi, _ = native
+    N, off, re, im = ham.xxz(20)
+    H = orc.OMatrix(N, N, off, re, im)
+    dH = _dev(capi, H)
+    out = ctypes.c_void_p()
+    capi.check(capi.lib().diaq_spgemm(dH.h, dH.h, 1, None, ctypes.byref(out)))
+    C = capi.Matrix(out)
+    fro = ctypes.c_double()
+    capi.check(capi.lib().diaq_frobenius(C.h, ctypes.byref(fro), None))
+    got_off = C.offsets()
+    del C
+    W = orc.product(H, H)
+    assert np.array_equal(got_off, W.off)
+    # numpy's pairwise sums (a sequential float64 sum of 689 M squares drifts by ~1e-11)
+    want = float(np.sqrt(np.sum(W.re ** 2) + np.sum(W.im ** 2)))
+    assert abs(fro.value - want) / want < 1e-12
