@@ -345,7 +345,7 @@ def run_ops(args):
     build.build()
     L = capi.lib()
     peak, peak_kind = peaks()
-    dfma_peak = 0.594e12   # FP64 FMA/s measured on the GB300s (throughput probe)
+    dfma_peak = 0.594e12   # FP64 FMA/s measured on a GB300 (throughput probe)
     use_ref = False
     try:
         use_ref = ref.available() and ref.lib() is not None

@@ -1,4 +1,4 @@
-"""Checkers for DiaQ's diagonal-sparse hot path -- TEST INFRASTRUCTURE ONLY.
+"""Oracles for DiaQ's diagonal-sparse hot path -- TEST INFRASTRUCTURE ONLY.
 
 ``oracle.oracle``    the C restatement (diaq_oracle.c) and the host algorithms over it.
 ``oracle.reference`` the reference's own CPU code, where it was built (oracle/_ref/).

@@ -1,7 +1,7 @@
 /*
  * diaq_oracle.c -- CPU restatement of DiaQ's diagonal-sparse hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: it is imported by tests/, by
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: it is imported by tests/, by
  * __graft_entry__.smoke() and by bench.py's cpu_baseline / reference leg, and never by the
  * product path (diaq_gb300/), which has no CPU fallback.
  *

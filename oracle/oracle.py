@@ -1,7 +1,7 @@
 """CPU oracle for DiaQ's diagonal-sparse hot path.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s
-cpu_baseline / reference leg, as the checker.  The product (``diaq_gb300``) never imports it.
+cpu_baseline / reference leg, to check results.  The product (``diaq_gb300``) never imports it.
 
 The numeric primitives are the C restatement in ``diaq_oracle.c`` (SpMV, the SpGEMM dry-run
 and numeric pass, norms, the time-evolution action).  The host-side algorithms that string them
