@@ -210,6 +210,9 @@ struct EpiHorner {
 // refreshes the float32 copy the next step starts from.
 constexpr int kNormBlocks = 256;
 
+// Recorded time steps a plan keeps (one per (dt, s, m, state pointers, ld)).
+constexpr size_t kMaxGraphs = 16;
+
 __global__ void norm_partial_kernel(const double *__restrict__ pr, const double *__restrict__ pi, int64_t n,
                                     double *__restrict__ part) {
     const int q = blockIdx.y;
@@ -429,7 +432,7 @@ struct EvolvePlan {
             return std::tie(dt, sl, m, pr, pi, ld) < std::tie(o.dt, o.sl, o.m, o.pr, o.pi, o.ld);
         }
     };
-    std::map<Key, cudaGraphExec_t> graphs;
+    std::map<Key, cudaGraphExec_t> graphs;   // one recorded step per key, at most kMaxGraphs
     int launches_per_step = 0;
     SpmvCfg cfg;          // launch shape of the term kernel
     bool tuned = false;   // cfg chosen (by the autotuner or the caller)
@@ -441,6 +444,7 @@ struct EvolvePlan {
     cudaEvent_t err_ev = nullptr; // ... and the event that says it has landed
     int sp = 4;           // interleaved layout: nrhs rounded up to a power of two >= 4 (<= 32 used)
     int64_t n_pad = 0;    // rows rounded up to a multiple of 32
+    double *stage = nullptr;  // device copy of the states for diaq_evolve_run_host, 2 * nrhs * n
 
     bool f32() const { return mode == DIAQ_EVOLVE_MIXED || mode == DIAQ_EVOLVE_HORNER; }
     bool interleaved() const { return f32() && cfg.pipe >= 6; }
@@ -455,6 +459,7 @@ struct EvolvePlan {
         if (err) cudaFree(err);
         if (err_host) cudaFreeHost(err_host);
         if (err_ev) cudaEventDestroy(err_ev);
+        if (stage) cudaFree(stage);
         if (Hc) destroy(Hc);
         if (s) cudaStreamDestroy(s);
     }
@@ -937,6 +942,13 @@ static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt
     const EvolvePlan::Key key{dt, sl, m, pr, pi, ld};
     auto it = P.graphs.find(key);
     if (it == P.graphs.end()) {
+        // a caller that passes ever new state pointers or time steps would otherwise grow the
+        // cache without end: past kMaxGraphs the recorded steps are dropped (an executable graph
+        // still in flight is released when it completes)
+        if (P.graphs.size() >= kMaxGraphs) {
+            for (auto &kv : P.graphs) cudaGraphExecDestroy(kv.second);
+            P.graphs.clear();
+        }
         // record one step on the plan's own stream (capture needs a stream other than the
         // legacy default); nothing runs during capture
         cudaGraph_t g = nullptr;
@@ -1042,8 +1054,10 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
     if (!psi_re || !psi_im) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
     const size_t cnt = (size_t)E->nrhs * (size_t)E->n;
     if (cnt == 0) return DIAQ_OK;
-    double *d = nullptr;
-    DQ_CUDA(cudaMalloc(&d, 2 * cnt * sizeof(double)));
+    // the device copy of the states is the plan's own, allocated on the first call and kept, so
+    // that later calls allocate nothing and find the step recorded for it
+    if (!E->stage) DQ_CUDA(cudaMalloc(&E->stage, 2 * cnt * sizeof(double)));
+    double *d = E->stage;
     cudaError_t e = cudaMemcpy(d, psi_re, cnt * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d + cnt, psi_im, cnt * sizeof(double), cudaMemcpyHostToDevice);
     int st = e == cudaSuccess ? DIAQ_OK : cuda_status(e, "evolve upload", __FILE__, __LINE__);
@@ -1053,7 +1067,6 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
         if (e == cudaSuccess) e = cudaMemcpy(psi_im, d + cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) st = cuda_status(e, "evolve download", __FILE__, __LINE__);
     }
-    cudaFree(d);
     return st;
 }
 

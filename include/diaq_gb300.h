@@ -242,12 +242,14 @@ int diaq_evolve_destroy(diaq_evolve_t E);
 /* Advance the nrhs states in place by `steps` time steps of dt, each 2^substeps_log2 sub-steps
  * of m Taylor terms.  psi_re/psi_im: float64 device arrays, state q at psi[q*ld ..]; ld must be
  * N.  The first call for a given (dt, s, m, psi) records one step as a CUDA graph; every step is
- * a replay.  Asynchronous on stream. */
+ * a replay.  A plan keeps up to 16 recorded steps and drops them all when a 17th is needed.
+ * Asynchronous on stream. */
 int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld, double dt,
                     int64_t steps, int substeps_log2, int m, void *stream);
 
 /* diaq_evolve_run with host arrays: the nrhs states (state q at psi[q*N ..]) are copied to the
- * device, advanced, and copied back.  Synchronous. */
+ * device, advanced, and copied back.  Synchronous.  The device copy of the states belongs to the
+ * plan: allocated by the first call, reused by the later ones, freed with the plan. */
 int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
                          int substeps_log2, int m);
 

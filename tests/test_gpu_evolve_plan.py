@@ -92,6 +92,43 @@ def test_repeated_runs_reuse_graph(native):
     assert maxrel(got[0], orc.ham_sim(A, P[0], 0.3, 6, 10)) < 1e-12
 
 
+def test_graph_cache_is_bounded(native):
+    """A new time step per call records a new step each time; past the plan's limit of 16 the
+    recorded steps are dropped and recorded again, and every result still follows the oracle."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 10, 2, capi.EVOLVE_C128)
+    want = [P[0], P[1]]
+    for i in range(20):
+        dt = 0.01 + 0.001 * i
+        E.run(pr, pi, A.rows, dt, 1, 0, 10)
+        want = [orc.ham_sim(A, w, dt, 1, 10) for w in want]
+    got = _result(pr, pi)
+    for q in range(2):
+        assert maxrel(got[q], want[q]) < 1e-12, q
+
+
+@pytest.mark.parametrize("mode", ["c128", "horner"])
+def test_run_host_calls_in_a_row(native, mode):
+    """diaq_evolve_run_host keeps its device copy of the states between calls: two calls in a row
+    (2 then 3 steps) equal 5 steps of the oracle (c128: 1e-12; the float32 Horner form: the 1e-6
+    bar)."""
+    capi, _ = native
+    N, off, re, im = ham.xxz(10)
+    A = orc.OMatrix(N, N, off, re, im)
+    H = capi.Matrix.create(N, N, off, re, im)
+    E = capi.Evolve(H, 3, capi.EVOLVE_C128 if mode == "c128" else capi.EVOLVE_HORNER)
+    P = ham.random_state(N, 0, k=3)
+    hr = np.ascontiguousarray(P.real).ravel().copy()
+    hi = np.ascontiguousarray(P.imag).ravel().copy()
+    E.run_host(hr, hi, 0.05, 2, 1, 9)
+    E.run_host(hr, hi, 0.05, 3, 1, 9)
+    got = (hr + 1j * hi).reshape(3, N)
+    for q in range(3):
+        want = orc.ham_sim(A, P[q], 0.25, 5, 9, substeps=2)
+        tol = 1e-12 if mode == "c128" else 1e-6
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < tol, q
+
+
 def test_plan_rejects_bad_input(native):
     capi, _ = native
     M = capi.Matrix.create(4, 6, [0], np.ones(4), np.zeros(4))
