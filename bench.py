@@ -872,16 +872,17 @@ def run_ours(args, rank, world):
     e2e_plan = capi.Evolve(H, S, CHOSEN_MODE)
     for _ in range(W):   # the plan's device copy of the states and its graph, outside the timed region
         e2e_plan.run_host(hr, hi, DT, 1, s_c, m_c)
-    torch.cuda.synchronize()
+    _barrier(world)
     t0 = time.perf_counter()
     for _ in range(K):
         e2e_plan.run_host(hr, hi, DT, 1, s_c, m_c)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = _max_over_ranks(time.perf_counter() - t0, world, dev)
     # the reference API's own pattern (hamiltonian_simulation_cuda): one call, S states up, K steps,
     # S states down
+    _barrier(world)
     t0 = time.perf_counter()
     e2e_plan.run_host(hr, hi, DT, K, s_c, m_c)
-    e2e_one_s = time.perf_counter() - t0
+    e2e_one_s = _max_over_ranks(time.perf_counter() - t0, world, dev)
     del e2e_plan
 
     # ---- SpMV on its own, c128 (FP64-issue bound on GB300) ----
