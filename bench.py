@@ -977,6 +977,7 @@ def run_ours(args, rank, world):
                               "all stored values (w Σlen + 2 w N) per time, the dense-diagonal figure"},
         "spmv_c128f2": {"us": spmv_f2_us, "gbs": (16 * live + 32 * N) / spmv_f2_us / 1e3,
                         "frac": (16 * live + 32 * N) / spmv_f2_us / 1e3 / peak,
+                        "effective_gbs": (16 * total + 32 * N) / spmv_f2_us / 1e3,
                         "maxrel_vs_c128": f2_err, "reps": args.spmv_reps,
                         "note": "same matrix as float pairs (DIAQ_C128F2), float64 vectors; includes the split of x"},
         "e2e": {"value": world * S * K / e2e_s, "unit": "states·steps/s", "h2d_bytes_per_step": 16 * N * S,
