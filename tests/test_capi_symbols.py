@@ -65,3 +65,23 @@ def test_invalid_arguments_fail_without_a_gpu(lib):
     st = L.diaq_matrix_create(1 << 31, 1 << 31, 1, off.ctypes.data, None, None, 0, 0, None, ctypes.byref(out))
     assert st == 4 and b"below 2^31" in L.diaq_last_error()   # 32-bit row indices in the kernels
     assert L.diaq_batch_set_interleaved(None, 1) == 1
+
+
+def test_every_entry_point_rejects_null_arguments(lib):
+    """Every function of the header called with NULL handles and pointers and zero sizes returns
+    a status (DIAQ_OK for the destroy functions and empty work, else DIAQ_ERR_INVALID with a
+    message) without touching memory or the GPU."""
+    import ctypes
+
+    L = lib.lib()
+    not_status = {"diaq_last_error", "diaq_version", "diaq_mlp_num_params", "diaq_evolve_launches_per_step"}
+    for name, (_, args) in sorted(lib.SIGNATURES.items()):
+        if name in not_status:
+            continue
+        vals = [0.0 if a in (ctypes.c_double, ctypes.c_float) else None if a is ctypes.c_void_p else 0 for a in args]
+        st = getattr(L, name)(*vals)
+        if name.endswith("_destroy") or name == "diaq_spmm_dia_device":   # NULL / empty: nothing to do
+            assert st == 0, name
+        else:
+            assert st == 1, (name, st)
+            assert L.diaq_last_error(), name
