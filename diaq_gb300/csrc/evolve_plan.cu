@@ -931,6 +931,8 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
 static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt, int64_t steps, int sl, int m,
                     cudaStream_t user) {
     if (steps < 0 || m < 0 || sl < 0 || sl > 20) return set_error(DIAQ_ERR_INVALID, "evolve: bad steps / s / m");
+    // dt keys the recorded steps: a NaN would compare equal to every key and replay another dt
+    if (!std::isfinite(dt)) return set_error(DIAQ_ERR_INVALID, "evolve: dt must be finite");
     if (!pr || !pi) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
     if (steps == 0 || m == 0 || P.n == 0) return DIAQ_OK;
     // an earlier run's bulk-copy kernel gave up a wait (the copy of its flag has landed)

@@ -137,6 +137,10 @@ def test_plan_rejects_bad_input(native):
     S = capi.Matrix.create(4, 4, [0], np.ones(4), np.zeros(4), precision=capi.C64)
     with pytest.raises(capi.DiaqError, match="c128"):
         capi.Evolve(S, 1)
+    A, E, P, pr, pi = _setup(capi, 6, 1, capi.EVOLVE_C128)
+    E.run(pr, pi, A.rows, 0.05, 1, 0, 8)
+    with pytest.raises(capi.DiaqError, match="finite"):   # never a replay of the 0.05 step
+        E.run(pr, pi, A.rows, float("nan"), 1, 0, 8)
 
 
 @pytest.mark.parametrize("cfg", [(8, 1, 0), (8, 2, 0), (8, 4, 0), (4, 2, 0), (4, 4, 0), (2, 4, 0), (1, 4, 0),
