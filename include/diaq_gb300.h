@@ -243,7 +243,7 @@ int diaq_evolve_destroy(diaq_evolve_t E);
  * of m Taylor terms.  psi_re/psi_im: float64 device arrays, state q at psi[q*ld ..]; ld must be
  * N.  The first call for a given (dt, s, m, psi) records one step as a CUDA graph; every step is
  * a replay.  A plan keeps up to 16 recorded steps and drops them all when a 17th is needed.
- * Asynchronous on stream. */
+ * dt must be finite.  Asynchronous on stream. */
 int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld, double dt,
                     int64_t steps, int substeps_log2, int m, void *stream);
 
