@@ -33,3 +33,27 @@ def test_reference_arm_other_ranks_exit_quietly():
     p = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert p.returncode == 0, p.stderr[-2000:]
     assert not [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+
+
+def test_reference_and_port_time_the_same_step():
+    """The arm's two kinds compute the same time step: the reference's rule over 2^s steps of
+    dt / 2^s (oracle/_ref, where the reference sources were built) and the oracle's one step of
+    dt in 2^s sub-steps."""
+    import numpy as np
+    import pytest
+
+    from conftest import maxrel
+    from diaq_gb300 import hamiltonians as ham
+    from oracle import oracle as orc
+    from oracle import reference as ref
+
+    if not ref.available():
+        pytest.skip("reference CPU library not built here")
+    N, off, re, im = ham.xxz(10)
+    H = orc.OMatrix(N, N, off, re, im)
+    p = ham.random_state(N, 0)
+    for s, m in ((0, 12), (2, 10)):
+        a = ref.ham_sim(H, p, 0.05, 1 << s, m)
+        b = orc.ham_sim(H, p, 0.05, 1, m, substeps=1 << s)
+        assert maxrel(a, b) < 1e-13, (s, m)
+        assert np.linalg.norm(a) > 0.99
