@@ -87,7 +87,7 @@ int norm1_est(const Matrix &A, double *out, cudaStream_t s) {
     *out = 0.0;
     if (A.nd == 0 || A.cols == 0) return DIAQ_OK;
     unsigned long long *d = nullptr;
-    DQ_CUDA(cudaMallocAsync(&d, sizeof(unsigned long long), s));
+    DQ_CUDA(dev_malloc_async(&d, sizeof(unsigned long long), s));
     cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), s);
     if (e == cudaSuccess) {
         const unsigned grid = (unsigned)((A.cols + 255) / 256);
@@ -112,7 +112,7 @@ int frobenius(const Matrix &A, double *out, cudaStream_t s) {
     if (A.capacity == 0) return DIAQ_OK;
     const int nblk = (int)std::min<int64_t>((A.capacity + 255) / 256, 2 * num_sms());
     double *d = nullptr;
-    DQ_CUDA(cudaMallocAsync(&d, sizeof(double) * (nblk + 1), s));
+    DQ_CUDA(dev_malloc_async(&d, sizeof(double) * (nblk + 1), s));
     if (A.prec == DIAQ_C128)
         sumsq_partial_kernel<double><<<nblk, 256, 0, s>>>((const double *)A.re, (const double *)A.im, A.capacity, d + 1);
     else
@@ -215,7 +215,7 @@ int union_add(const Matrix &A, const Matrix &B, double sign, cudaStream_t s, Mat
         return DIAQ_OK;
     }
     int2 *d = nullptr;
-    cudaError_t e = cudaMallocAsync(&d, sizeof(int2) * slots.size(), s);
+    cudaError_t e = dev_malloc_async(&d, sizeof(int2) * slots.size(), s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d, slots.data(), sizeof(int2) * slots.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
         int64_t maxlen = 1;
@@ -508,6 +508,36 @@ int diaq_expm_negative(diaq_matrix_t A, double t, int max_iterations, double sca
                          terms_out));
     *U = handle(M);
     return DIAQ_OK;
+}
+
+// The reference's Pade exponential (src/spME.cpp:298-445).  What it does, observed on its own CPU
+// build: a matrix with one diagonal gets the single-diagonal exponential (:309-336, the rule of
+// single_diag_exp); any other matrix fails.  A rectangular one fails in the first addMatrixScaled
+// (src/diaQMatrix.hpp:1061-1072, shape check).  A square one reaches the inverse of V - U
+// (:433, src/spME.cpp:521-589), which solves for every column and stores each solution with
+// set(row, col) into a matrix made by the diaQMatrix(s, numDiags) constructor -- about N of the
+// 2N - 1 diagonals -- so the first entry on a missing diagonal throws (src/diaQMatrix.hpp:676-688);
+// for N >= 2 that happens in every case.  An empty square matrix makes V - U the zero diagonal,
+// whose inverse throws "Matrix is singular" from inside an OpenMP loop, which ends the reference's
+// process; here it is an error status.  The arguments max_iterations, scale_cutoff and tolerance
+// only steer the series the reference builds before the inverse, so they change no result.
+int diaq_expm_negative_pade(diaq_matrix_t A, double t, int max_iterations, double scale_cutoff, double tolerance,
+                            void *stream, diaq_matrix_t *U) {
+    (void)max_iterations;
+    (void)scale_cutoff;
+    (void)tolerance;
+    if (!A || !U) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    if (A->prec == DIAQ_C128F2)
+        return set_error(DIAQ_ERR_UNSUPPORTED, "expm_negative_pade: convert a c128f2 matrix to c128 first");
+    if (A->nd == 1) {
+        Matrix *M = nullptr;
+        DQ_TRY(single_diag_exp(*A, 1, t, (cudaStream_t)stream, &M));
+        *U = handle(M);
+        return DIAQ_OK;
+    }
+    if (A->rows != A->cols) return set_error(DIAQ_ERR_INVALID, "addMatrixScaled: matrix shapes do not match");
+    if (A->nd == 0) return set_error(DIAQ_ERR_UNSUPPORTED, "Matrix is singular, cannot compute inverse.");
+    return set_error(DIAQ_ERR_UNSUPPORTED, "set: diagonal index not present in dIndices.");
 }
 
 int diaq_expm(diaq_matrix_t A, int max_iterations, double scale_cutoff, double tolerance, int prune,

@@ -331,6 +331,28 @@ def expm_negative(A: OMatrix, t: float, max_iterations=100, scale_cutoff=1.0, to
     return pow(U, 1 << s, prune_result)
 
 
+def expm_negative_pade(A: OMatrix, t: float, max_iterations=100, scale_cutoff=1.0, tolerance=1e-12):
+    """exp(-i t A) as the reference's Pade routine computes it (src/spME.cpp:298-445).
+
+    One diagonal: the single-diagonal exponential of :309-336 (the same rule as the Taylor path's).
+    Every other input fails there, and the messages are the reference's: a rectangular matrix in
+    addMatrixScaled's shape check (src/diaQMatrix.hpp:1061-1072); a square one with two or more
+    diagonals when the inverse of V - U (:433, :521-589) stores its solution with set(row, col)
+    into a matrix built by diaQMatrix(s, numDiags), which holds about N of the 2N - 1 diagonals
+    (src/diaQMatrix.hpp:68-81, :676-688); a square one with none at the inverse of the zero
+    diagonal ("Matrix is singular", thrown inside an OpenMP loop: the reference's process ends
+    there).  max_iterations, scale_cutoff and tolerance only steer the series built before the
+    inverse."""
+    if A.nd == 1:
+        U, _ = expm_negative_taylor(A, t, max_iterations, tolerance)
+        return U
+    if A.rows != A.cols:
+        raise RuntimeError("addMatrixScaled: matrix shapes do not match")
+    if A.nd == 0:
+        raise RuntimeError("Matrix is singular, cannot compute inverse.")
+    raise RuntimeError("set: diagonal index not present in dIndices.")
+
+
 def expm(A: OMatrix, max_iterations=100, scale_cutoff=1.0, tolerance=1e-12, prune_result=True):
     """exp(A) by Taylor + scaling and squaring (src/spME.cpp:13-150)."""
     if A.nd == 1:

@@ -149,6 +149,16 @@ void *ref_expm_negative(void *a, double t, int max_it, double cutoff, double tol
     }
 }
 
+// exp(-i t A) through diaq::expm_negative_pade (src/spME.cpp:298-445, its inverse :447-589).
+void *ref_expm_negative_pade(void *a, double t, int max_it, double cutoff, double tol) {
+    try {
+        return new Held{diaq::expm_negative_pade(static_cast<Held *>(a)->m, t, max_it, cutoff, tol)};
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return nullptr;
+    }
+}
+
 // exp(A) through diaq::expm_taylor_scaled (src/spME.cpp:13-80).
 void *ref_expm(void *a, int max_it, double cutoff, double tol) {
     try {

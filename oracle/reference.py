@@ -15,6 +15,15 @@ from .oracle import OMatrix, _p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libdiaq_ref.so")
+# Where the reference tree lies on a host that has it: the environment variable DIAQ_REFERENCE,
+# else the default below.  The one place that names it; the Makefile and the fixture script take
+# it from here.
+REFERENCE_ROOT = os.environ.get("DIAQ_REFERENCE", "/root/reference")
+
+
+def reference_present() -> bool:
+    """True where the reference's CPU sources can be compiled (its src/ directory exists)."""
+    return os.path.isdir(os.path.join(REFERENCE_ROOT, "src"))
 _lib = None
 
 
@@ -43,6 +52,8 @@ def lib():
         L.ref_pow.argtypes = [P, ctypes.c_int]
         L.ref_expm_negative.restype = P
         L.ref_expm_negative.argtypes = [P, f64, ctypes.c_int, f64, f64]
+        L.ref_expm_negative_pade.restype = P
+        L.ref_expm_negative_pade.argtypes = [P, f64, ctypes.c_int, f64, f64]
         L.ref_expm.restype = P
         L.ref_expm.argtypes = [P, ctypes.c_int, f64, f64]
         L.ref_norm1_est.restype = f64
@@ -102,6 +113,12 @@ def pow(A: OMatrix, n: int) -> OMatrix:
 def expm_negative(A: OMatrix, t, max_iterations=100, scale_cutoff=1.0, tolerance=1e-12) -> OMatrix:
     a = RefMatrix.from_omatrix(A)
     return RefMatrix(lib().ref_expm_negative(a.h, t, max_iterations, scale_cutoff, tolerance)).to_omatrix()
+
+
+def expm_negative_pade(A: OMatrix, t, max_iterations=100, scale_cutoff=1.0, tolerance=1e-12) -> OMatrix:
+    """src/spME.cpp:298-445; raises RuntimeError with the reference's message where it throws."""
+    a = RefMatrix.from_omatrix(A)
+    return RefMatrix(lib().ref_expm_negative_pade(a.h, t, max_iterations, scale_cutoff, tolerance)).to_omatrix()
 
 
 def expm(A: OMatrix, max_iterations=100, scale_cutoff=1.0, tolerance=1e-12) -> OMatrix:

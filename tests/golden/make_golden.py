@@ -115,11 +115,15 @@ def rand_dia(rng, r, c, n_diags=None, fill=0.7):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=ref.REFERENCE_ROOT, help="the reference tree (default: $DIAQ_REFERENCE)")
     ap.add_argument("--skip-slow", action="store_true")
+    ap.add_argument("--only", choices=["pade"], help="write only this fixture file")
     args = ap.parse_args()
     if not ref.available():
         sys.exit("build the reference CPU library first: make -C oracle ref")
+    if args.only == "pade":
+        write_pade()
+        return
 
     # 1. hand-written SpGEMM cases
     cases = parse_spgemm_cases(os.path.join(args.ref, "cpp_tests", "test_main.cpp"))
@@ -195,6 +199,41 @@ def main():
         api[f"C{trial}"], api[f"Coff{trial}"], api[f"y{trial}"] = C.to_dense(), C.off, ref.spmv(oa, x)
     np.savez_compressed(os.path.join(HERE, "api_random.npz"), **api)
     print("api_random: 25")
+
+    write_pade()
+
+
+def pade_cases():
+    """Inputs of the Pade fixtures: (name, matrix, t).  One-diagonal matrices (main, upper, lower,
+    rectangular, all-zero) and matrices the reference's routine rejects."""
+    rng = np.random.default_rng(11)
+    cases = []
+    for name, n, off in (("main6", 6, 0), ("upper6", 6, 2), ("lower6", 6, -1), ("main64", 64, 0)):
+        L = n - abs(off)
+        cases.append((name, orc.OMatrix(n, n, [off], rng.uniform(-2, 2, L), rng.uniform(-0.5, 0.5, L)), 0.7))
+    cases.append(("rect3x5", orc.OMatrix(3, 5, [1], np.array([1.0, 2.0, 3.0]), np.zeros(3)), 0.5))
+    cases.append(("zero3", orc.OMatrix(3, 3, [0], np.zeros(3), np.zeros(3)), 0.5))
+    cases.append(("tfim3", omat(ham.tfim(3)), 0.1))
+    cases.append(("xxz4", omat(ham.xxz(4)), 2.0))
+    cases.append(("two2x2", orc.OMatrix(2, 2, [0, -1], np.array([1.0, 2.0, 0.5]), np.zeros(3)), 0.3))
+    cases.append(("rect3x5two", orc.OMatrix(3, 5, [0, 1], np.arange(1.0, 7.0), np.zeros(6)), 0.5))
+    return cases
+
+
+def write_pade():
+    """6. The reference's Pade exponential (src/spME.cpp:298-445) on pade_cases(): the result
+    (offsets, packed values) or the message of the exception it raises."""
+    pd = {}
+    for name, A, t in pade_cases():
+        pd[f"{name}_shape"] = np.array([A.rows, A.cols])
+        pd[f"{name}_off"], pd[f"{name}_re"], pd[f"{name}_im"], pd[f"{name}_t"] = A.off, A.re, A.im, np.array(t)
+        try:
+            U = ref.expm_negative_pade(A, t)
+            pd[f"{name}_U_off"], pd[f"{name}_U_re"], pd[f"{name}_U_im"] = U.off, U.re, U.im
+        except RuntimeError as e:
+            pd[f"{name}_error"] = np.array(str(e))
+    np.savez_compressed(os.path.join(HERE, "pade.npz"), **pd)
+    print("pade:", len(pade_cases()))
 
 
 def OScaled(A: orc.OMatrix, s: float) -> orc.OMatrix:

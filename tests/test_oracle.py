@@ -103,6 +103,26 @@ def test_ham_sim(name):
     assert maxrel(orc.ham_sim(A, p, 0.2, 3, 100), g[f"{name}_t0.2_r3_m100"]) < 1e-13
 
 
+@pytest.mark.parametrize("name", ["tfim10", "xxz10"])
+def test_timing_restatement_against_fixtures(name):
+    """The timing restatement of the reference's CPU scheme (bench.py's CPU baseline) computes the
+    same evolution as the reference's own CPU build (the fixtures) and the parity oracle, and its
+    SpMV equals the oracle's to rounding, with tiles shorter than the diagonals."""
+    from oracle import timing as tim
+
+    g = golden("ham_sim.npz")
+    A = omat(ham.tfim(10) if name == "tfim10" else ham.xxz(10))
+    p = g[f"{name}_psi0"]
+    q = p
+    for _ in range(5):   # 5 steps of dt = 0.1, 20 terms each: the fixture's t = 0.5, r = 5
+        q = tim.ham_sim(A, q, 0.1, 1, 20)
+    assert maxrel(q, g[f"{name}_t0.5_r5_m20"]) < 1e-13
+    assert maxrel(tim.ham_sim(A, p, 0.1, 4, 12), orc.ham_sim(A, p, 0.1, 1, 12, substeps=4)) < 1e-13
+    assert tim.tile() < A.rows
+    x = ham.random_state(A.rows, 3)
+    assert maxrel(tim.spmv(A, x), orc.spmv(A, x)) < 1e-14
+
+
 def test_ham_sim_edges():
     A = omat(ham.tfim(6))
     p = ham.random_state(64, 1)
@@ -173,3 +193,30 @@ def test_mlp_oracle_gradient_finite_differences():
         pm[idx] -= h
         fd = (omlp.loss_and_grad(pp, X, ys, ym)[0].mean() - omlp.loss_and_grad(pm, X, ys, ym)[0].mean()) / (2 * h)
         assert abs(fd - g[idx]) <= 1e-7 + 1e-5 * abs(g[idx])
+
+
+def _pade_inputs(g):
+    names = sorted({k[: -len("_shape")] for k in g.files if k.endswith("_shape")})
+    for name in names:
+        rows, cols = (int(v) for v in g[f"{name}_shape"])
+        A = orc.OMatrix(rows, cols, g[f"{name}_off"], g[f"{name}_re"], g[f"{name}_im"])
+        yield name, A, float(g[f"{name}_t"])
+
+
+def test_pade_against_reference():
+    """src/spME.cpp:298-445 run on the reference's own build (tests/golden/pade.npz): one-diagonal
+    results to the last bit of the fixture's libm, and the same exception messages elsewhere."""
+    g = golden("pade.npz")
+    seen_error = seen_value = 0
+    for name, A, t in _pade_inputs(g):
+        if f"{name}_error" in g.files:
+            with pytest.raises(RuntimeError) as ei:
+                orc.expm_negative_pade(A, t)
+            assert str(ei.value) == str(g[f"{name}_error"]), name
+            seen_error += 1
+        else:
+            U = orc.expm_negative_pade(A, t)
+            assert np.array_equal(U.off, g[f"{name}_U_off"]), name
+            assert maxrel(U.re + 1j * U.im, g[f"{name}_U_re"] + 1j * g[f"{name}_U_im"]) < 1e-15, name
+            seen_value += 1
+    assert seen_error >= 4 and seen_value >= 5
