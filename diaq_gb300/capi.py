@@ -28,6 +28,7 @@ SIGNATURES = {
     "diaq_matrix_destroy": (INT, [P]),
     "diaq_matrix_info": (INT, [P, P, P, P, P, P]),
     "diaq_matrix_offsets": (INT, [P, P]),
+    "diaq_matrix_live_values": (INT, [P, P, P]),
     "diaq_matrix_download": (INT, [P, P, P, INT, P]),
     "diaq_matrix_copy": (INT, [P, P, P]),
     "diaq_matrix_convert": (INT, [P, INT, P, P]),
@@ -48,6 +49,7 @@ SIGNATURES = {
     "diaq_pow": (INT, [P, INT, INT, P, P]),
     "diaq_expm_negative": (INT, [P, F64, INT, F64, F64, INT, P, P, P, P]),
     "diaq_expm": (INT, [P, INT, F64, F64, INT, P, P]),
+    "diaq_expm_negative_pade": (INT, [P, F64, INT, F64, F64, P, P]),
     "diaq_ham_sim": (INT, [P, P, P, F64, I64, INT, P, P, P]),
     "diaq_ham_sim_host": (INT, [P, P, P, F64, I64, INT, P, P]),
     "diaq_select_sm": (INT, [F64, F64, F64, F64, INT, P, P]),
@@ -59,6 +61,8 @@ SIGNATURES = {
     "diaq_evolve_config": (INT, [P, P, P, P]),
     "diaq_evolve_set_renormalize": (INT, [P, INT]),
     "diaq_evolve_run_host": (INT, [P, P, P, F64, I64, INT, INT]),
+    "diaq_evolve_check": (INT, [P]),
+    "diaq_evolve_set_wait_limit": (INT, [P, I64]),
     "diaq_select_sm_min_cost": (INT, [F64, F64, F64, INT, INT, P, P]),
     "diaq_ham_sim_noalloc": (INT, [P, P, P, F64, I64, INT, P, P, P]),
     "diaq_matrix_from_pauli": (INT, [INT, I32, P, P, P, P, INT, P, P]),
@@ -165,6 +169,12 @@ class Matrix:
         check(lib().diaq_matrix_offsets(self.h, off.ctypes.data))
         return off[:nd]
 
+    def live_values(self) -> int:
+        """Stored values in 32-row tiles that hold a nonzero (what the SpMV kernels read)."""
+        out = ctypes.c_int64()
+        check(lib().diaq_matrix_live_values(self.h, ctypes.byref(out), None))
+        return out.value
+
     def download(self):
         """(offsets, re, im) packed, float64, on the host."""
         rows, cols, nd, total, _ = self.info()
@@ -254,6 +264,14 @@ class Evolve:
 
     def set_renormalize(self, on: bool = True):
         check(lib().diaq_evolve_set_renormalize(self.h, 1 if on else 0))
+
+    def check(self):
+        """Wait for the last run; raise if a bounded wait of a bulk-copy kernel gave up in it."""
+        check(lib().diaq_evolve_check(self.h))
+
+    def set_wait_limit(self, wait_ns: int):
+        """Time bound of one device-side wait of the bulk-copy kernels, in ns (0: the default)."""
+        check(lib().diaq_evolve_set_wait_limit(self.h, int(wait_ns)))
 
     def launches_per_step(self) -> int:
         return lib().diaq_evolve_launches_per_step(self.h)

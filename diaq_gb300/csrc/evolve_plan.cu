@@ -212,6 +212,10 @@ constexpr int kNormBlocks = 256;
 
 // Recorded time steps a plan keeps (one per (dt, s, m, state pointers, ld)).
 constexpr size_t kMaxGraphs = 16;
+// Bounds of the bulk-copy kernels' waits (variants 10, 11): one wait for a shared-memory stage, and
+// the producer's wait for its copies in flight before its block may finish.
+constexpr uint64_t kWaitNs = 20000000ull;   // 20 ms
+constexpr uint64_t kDrainNs = 10000000ull;  // 10 ms
 
 __global__ void norm_partial_kernel(const double *__restrict__ pr, const double *__restrict__ pi, int64_t n,
                                     double *__restrict__ part) {
@@ -423,6 +427,10 @@ struct EvolvePlan {
     int64_t n = 0;
     void *buf = nullptr;         // work vectors
     cudaStream_t s = nullptr;    // capture stream
+    // diaq_evolve_run_host: the real and the imaginary planes are copied on two streams at once
+    // (two copy engines), the run itself on the first
+    cudaStream_t hs[2] = {nullptr, nullptr};
+    cudaEvent_t hev[2] = {nullptr, nullptr};
     struct Key {
         double dt;
         int sl, m;
@@ -439,9 +447,10 @@ struct EvolvePlan {
     bool renorm = false;  // rescale every state to norm 1 (float64) after each step
     double *part = nullptr;  // renormalisation partial sums, nrhs * kNormBlocks
     uint32_t *tmask = nullptr;  // zero-tile mask of the matrix the term kernels read (Hc, or H for C128)
-    int *err = nullptr;           // bounded waits of the bulk-copy kernel (variant 10) record here
+    int *err = nullptr;           // bounded waits of the bulk-copy kernels (variants 10, 11) record here
     int *err_host = nullptr;      // pinned copy of *err taken after each run
     cudaEvent_t err_ev = nullptr; // ... and the event that says it has landed
+    uint64_t wait_ns = kWaitNs;   // bound of one wait of the bulk-copy kernels
     int sp = 4;           // interleaved layout: nrhs rounded up to a power of two >= 4 (<= 32 used)
     int64_t n_pad = 0;    // rows rounded up to a multiple of 32
     double *stage = nullptr;  // device copy of the states for diaq_evolve_run_host, 2 * nrhs * n
@@ -462,6 +471,10 @@ struct EvolvePlan {
         if (stage) cudaFree(stage);
         if (Hc) destroy(Hc);
         if (s) cudaStreamDestroy(s);
+        for (int j = 0; j < 2; ++j) {
+            if (hs[j]) cudaStreamDestroy(hs[j]);
+            if (hev[j]) cudaEventDestroy(hev[j]);
+        }
     }
 };
 
@@ -507,18 +520,20 @@ int launch_il(const EvolvePlan &P, const float *xr, const float *xi, const Epi &
         const int64_t mw = tile_mask_words(P.n);
         const DiagMeta *md = P.Hc->d_meta;
         const int nd = P.Hc->nd;
+        // a copy lands within microseconds: the drain bound is generous whatever the wait bound
+        const uint64_t wn = P.wait_ns, dn = std::max<uint64_t>(P.wait_ns, kDrainNs);
         if (G == 8 && win)
             dia_spmv_tma_kernel<Epi, 8, true, 4><<<gt, kTmaThreads, smem, P.s>>>(md, nd, are, aim, P.n, P.n_pad, xr, xi,
-                                                                                 P.tmask, mw, e, P.err);
+                                                                                 P.tmask, mw, e, P.err, wn, dn);
         else if (G == 8)
             dia_spmv_tma_kernel<Epi, 8, false, 8><<<gt, kTmaThreads, smem, P.s>>>(md, nd, are, aim, P.n, P.n_pad, xr, xi,
-                                                                                  P.tmask, mw, e, P.err);
+                                                                                  P.tmask, mw, e, P.err, wn, dn);
         else if (win)
             dia_spmv_tma_kernel<Epi, 4, true, 4><<<gt, kTmaThreads, smem, P.s>>>(md, nd, are, aim, P.n, P.n_pad, xr, xi,
-                                                                                 P.tmask, mw, e, P.err);
+                                                                                 P.tmask, mw, e, P.err, wn, dn);
         else
             dia_spmv_tma_kernel<Epi, 4, false, 8><<<gt, kTmaThreads, smem, P.s>>>(md, nd, are, aim, P.n, P.n_pad, xr, xi,
-                                                                                  P.tmask, mw, e, P.err);
+                                                                                  P.tmask, mw, e, P.err, wn, dn);
         DQ_CUDA(cudaGetLastError());
         return DIAQ_OK;
     }
@@ -573,13 +588,13 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     const size_t bytes = mode == DIAQ_EVOLVE_C128 ? 6 * vec * sizeof(double)
                                                   : 8 * std::max<size_t>((size_t)P->sp * (size_t)P->n_pad,
                                                                          vec) * sizeof(float);
-    if (e == cudaSuccess && bytes) e = cudaMalloc(&P->buf, bytes);
+    if (e == cudaSuccess && bytes) e = dev_malloc(&P->buf, bytes);
     if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
     if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
     if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128)
         st = mode == DIAQ_EVOLVE_HORNER ? allow_tma_smem<EpiHornerIL>() : allow_tma_smem<EpiMixedIL>();
     if (st == DIAQ_OK) {
-        e = cudaMalloc(&P->err, sizeof(int));
+        e = dev_malloc(&P->err, sizeof(int));
         if (e == cudaSuccess) e = cudaMemsetAsync(P->err, 0, sizeof(int), P->s);
         if (e == cudaSuccess) e = cudaMallocHost(&P->err_host, sizeof(int));
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->err_ev, cudaEventDisableTiming);
@@ -589,7 +604,7 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     if (st == DIAQ_OK && H.nd > 0) {
         // the mask of the plan's own c64 copy is built once; that of the caller's c128 matrix
         // again at every run (its values may have changed)
-        e = cudaMalloc(&P->tmask, sizeof(uint32_t) * (size_t)H.nd * (size_t)tile_mask_words(H.rows));
+        e = dev_malloc(&P->tmask, sizeof(uint32_t) * (size_t)H.nd * (size_t)tile_mask_words(H.rows));
         if (e != cudaSuccess) st = cuda_status(e, "evolve plan mask", __FILE__, __LINE__);
         if (st == DIAQ_OK) st = build_tile_mask(P->Hc ? *P->Hc : H, P->tmask, P->s);
         if (st == DIAQ_OK && (e = cudaStreamSynchronize(P->s)) != cudaSuccess)
@@ -606,7 +621,7 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
 // The partial sums of the renormalisation; allocated before any step is recorded (no
 // allocation is allowed while a stream is being captured).
 static int ensure_renorm_buffer(EvolvePlan &P) {
-    if (P.renorm && !P.part) DQ_CUDA(cudaMalloc(&P.part, sizeof(double) * kNormBlocks * P.nrhs));
+    if (P.renorm && !P.part) DQ_CUDA(dev_malloc(&P.part, sizeof(double) * kNormBlocks * P.nrhs));
     return DIAQ_OK;
 }
 
@@ -771,6 +786,34 @@ static int fp32_state(EvolvePlan &P, const double *pr, const double *pi, cudaStr
     return DIAQ_OK;
 }
 
+// Clear the bulk-copy kernels' error flag (device and pinned copy).
+static int clear_wait_error(EvolvePlan &P) {
+    *P.err_host = 0;
+    DQ_CUDA(cudaMemsetAsync(P.err, 0, sizeof(int), P.s));
+    DQ_CUDA(cudaStreamSynchronize(P.s));
+    return DIAQ_OK;
+}
+
+// DIAQ_ERR_TIMEOUT, and the flag cleared, when a wait of a bulk-copy kernel (variants 10, 11) of
+// an earlier run gave up; that run's states are then not advanced correctly.  sync: wait for the
+// last run's copy of the flag; else look only if it has landed.
+static int take_wait_error(EvolvePlan &P, bool sync) {
+    if (sync) {
+        const cudaError_t e = cudaEventSynchronize(P.err_ev);
+        if (e != cudaSuccess) return cuda_status(e, "evolve: wait for the run", __FILE__, __LINE__);
+    } else if (cudaEventQuery(P.err_ev) != cudaSuccess) {
+        return DIAQ_OK;
+    }
+    const int code = *P.err_host;
+    if (code == 0) return DIAQ_OK;
+    DQ_TRY(clear_wait_error(P));
+    const char *what = code == 2 ? "a consumer warp's wait for a filled stage"
+                       : code == 1 ? "the producer's wait for a free stage"
+                                   : "the producer's wait for its copies in flight";
+    return set_error(DIAQ_ERR_TIMEOUT, std::string("evolve: the bulk-copy term kernel gave up ") + what +
+                                           " after its time bound; the states of that run are not valid");
+}
+
 // ---- autotuner ----------------------------------------------------------------------------------------
 // Candidate launch shapes (states per launch, rows per thread) are timed on two steps of the
 // caller's problem, run on scratch copies of the states (the caller's are not advanced), and the
@@ -850,8 +893,9 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
         cand = {{8, 1, 0}, {8, 2, 0}, {8, 4, 0}, {4, 2, 0}, {4, 4, 0}, {2, 4, 0}, {1, 4, 0},
                 {8, 4, 1}, {4, 4, 1}, {2, 4, 1}, {1, 4, 1},
                 {8, 4, 2}, {4, 4, 2}, {2, 4, 2}, {1, 4, 2}, {8, 4, 3}, {4, 4, 3}, {2, 4, 3},
-                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}, {4, 1, 10}, {4, 1, 11},
-                {4, 1, 12}};
+                {8, 4, 4}, {4, 4, 4}, {2, 4, 4}, {4, 1, 6}, {4, 1, 7}, {4, 1, 8}, {4, 1, 9}, {4, 1, 12}};
+    // (the bulk-copy variants 10 and 11 measured slower than 9 and 12 on every workload and stay
+    // selectable through diaq_evolve_set_config only)
     else
         cand = {{8, 1, 0}, {8, 2, 0}, {4, 2, 0}, {2, 2, 0}, {1, 2, 0}};
     // drop shapes with more states per launch than the plan has (same launches as a smaller one)
@@ -881,7 +925,7 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
     // scratch copies of the states
     const size_t cnt = (size_t)P.nrhs * (size_t)P.n;
     double *tmp = nullptr;
-    DQ_CUDA(cudaMalloc(&tmp, 2 * cnt * sizeof(double)));
+    DQ_CUDA(dev_malloc(&tmp, 2 * cnt * sizeof(double)));
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -911,6 +955,17 @@ static int autotune(EvolvePlan &P, double dt, int sl, int m, double *pr, double 
         }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
+        // a candidate whose bounded waits gave up is not eligible (its time means nothing)
+        int flag = 0;
+        e = cudaMemcpy(&flag, P.err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            st = cuda_status(e, "autotune", __FILE__, __LINE__);
+            break;
+        }
+        if (flag != 0) {
+            st = clear_wait_error(P);
+            continue;
+        }
         if (best < 0.f || ms < best) {
             best = ms;
             best_cfg = cand[c];
@@ -936,8 +991,7 @@ static int plan_run(EvolvePlan &P, double *pr, double *pi, int64_t ld, double dt
     if (!pr || !pi) return set_error(DIAQ_ERR_INVALID, "evolve: psi pointer is NULL");
     if (steps == 0 || m == 0 || P.n == 0) return DIAQ_OK;
     // an earlier run's bulk-copy kernel gave up a wait (the copy of its flag has landed)
-    if (cudaEventQuery(P.err_ev) == cudaSuccess && *P.err_host != 0)
-        return set_error(DIAQ_ERR_CUDA, "evolve: the bulk-copy term kernel timed out waiting on a shared-memory stage");
+    DQ_TRY(take_wait_error(P, false));
     if (!P.Hc && P.tmask) DQ_TRY(build_tile_mask(*P.H, P.tmask, user));
     DQ_TRY(ensure_renorm_buffer(P));
     if (!P.tuned) DQ_TRY(autotune(P, dt, sl, m, pr, pi, ld, user));
@@ -1029,7 +1083,26 @@ int diaq_evolve_set_config(diaq_evolve_t E, int states_per_block, int rows_per_t
     }
     for (auto &kv : E->graphs) cudaGraphExecDestroy(kv.second);
     E->graphs.clear();
+    // an error of the previous kernel is not carried over to the new one
+    DQ_CUDA(cudaEventSynchronize(E->err_ev));
+    return clear_wait_error(*E);
+}
+
+int diaq_evolve_set_wait_limit(diaq_evolve_t E, int64_t wait_ns) {
+    if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
+    if (wait_ns < 0) return set_error(DIAQ_ERR_INVALID, "evolve: the wait limit must be >= 0 nanoseconds");
+    const uint64_t w = wait_ns == 0 ? kWaitNs : (uint64_t)wait_ns;
+    if (w != E->wait_ns) {  // the bound is a kernel argument of the recorded steps
+        E->wait_ns = w;
+        for (auto &kv : E->graphs) cudaGraphExecDestroy(kv.second);
+        E->graphs.clear();
+    }
     return DIAQ_OK;
+}
+
+int diaq_evolve_check(diaq_evolve_t E) {
+    if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
+    return take_wait_error(*E, true);
 }
 
 int diaq_evolve_set_renormalize(diaq_evolve_t E, int on) {
@@ -1058,17 +1131,35 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
     if (cnt == 0) return DIAQ_OK;
     // the device copy of the states is the plan's own, allocated on the first call and kept, so
     // that later calls allocate nothing and find the step recorded for it
-    if (!E->stage) DQ_CUDA(cudaMalloc(&E->stage, 2 * cnt * sizeof(double)));
+    if (!E->stage) DQ_CUDA(dev_malloc(&E->stage, 2 * cnt * sizeof(double)));
+    for (int j = 0; j < 2; ++j) {
+        if (!E->hs[j]) DQ_CUDA(cudaStreamCreateWithFlags(&E->hs[j], cudaStreamNonBlocking));
+        if (!E->hev[j]) DQ_CUDA(cudaEventCreateWithFlags(&E->hev[j], cudaEventDisableTiming));
+    }
     double *d = E->stage;
-    cudaError_t e = cudaMemcpy(d, psi_re, cnt * sizeof(double), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d + cnt, psi_im, cnt * sizeof(double), cudaMemcpyHostToDevice);
+    cudaStream_t a = E->hs[0], b = E->hs[1];
+    const size_t bytes = cnt * sizeof(double);
+    // up: re on a, im on b at the same time; the run on a once both have landed
+    cudaError_t e = cudaMemcpyAsync(d, psi_re, bytes, cudaMemcpyHostToDevice, a);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d + cnt, psi_im, bytes, cudaMemcpyHostToDevice, b);
+    if (e == cudaSuccess) e = cudaEventRecord(E->hev[1], b);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(a, E->hev[1], 0);
     int st = e == cudaSuccess ? DIAQ_OK : cuda_status(e, "evolve upload", __FILE__, __LINE__);
-    if (st == DIAQ_OK) st = plan_run(*E, d, d + cnt, E->n, dt, steps, substeps_log2, m, nullptr);
+    if (st == DIAQ_OK) st = plan_run(*E, d, d + cnt, E->n, dt, steps, substeps_log2, m, a);
     if (st == DIAQ_OK) {
-        e = cudaMemcpy(psi_re, d, cnt * sizeof(double), cudaMemcpyDeviceToHost);
-        if (e == cudaSuccess) e = cudaMemcpy(psi_im, d + cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost);
+        // down: both planes once the run has finished, again on the two streams
+        e = cudaEventRecord(E->hev[0], a);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b, E->hev[0], 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(psi_re, d, bytes, cudaMemcpyDeviceToHost, a);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(psi_im, d + cnt, bytes, cudaMemcpyDeviceToHost, b);
         if (e != cudaSuccess) st = cuda_status(e, "evolve download", __FILE__, __LINE__);
     }
+    // synchronous: both streams drained whatever happened above
+    const cudaError_t ea = cudaStreamSynchronize(a), eb = cudaStreamSynchronize(b);
+    if (st == DIAQ_OK && ea != cudaSuccess) st = cuda_status(ea, "evolve run_host", __FILE__, __LINE__);
+    if (st == DIAQ_OK && eb != cudaSuccess) st = cuda_status(eb, "evolve run_host", __FILE__, __LINE__);
+    // the run has finished: a wait that gave up in it is reported now, not at the next call
+    if (st == DIAQ_OK) st = take_wait_error(*E, true);
     return st;
 }
 

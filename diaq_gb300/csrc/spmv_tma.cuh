@@ -12,10 +12,12 @@
 // released it.  Up to S diagonals of every block are in flight with no consumer waiting on
 // global memory.
 //
-// Every wait is bounded: after kTmaSpinLimit polls the waiting warp records an error in *err and
-// leaves -- the producer only after waiting (bounded again) for the copies it has in flight, so
-// that no copy lands in the shared memory of a finished block; the plan reports the error on its
-// next run.
+// Every wait is bounded in time (%globaltimer, nanoseconds): a consumer warp that waits longer
+// than `wait_ns` for a stage records an error in *err and leaves; the producer gives up a wait for
+// a free stage after `wait_ns` as well.  On every exit path the producer first waits -- bounded by
+// `drain_ns`, which the launcher sets well above the microseconds a copy takes -- for the last
+// fill of every stage it used, so no copy lands in the shared memory of a finished block.  The
+// plan reports the error to the caller (diaq_evolve_check, or the next run).
 #pragma once
 
 #include "spmv_il.cuh"
@@ -25,7 +27,6 @@ namespace diaq_gb300 {
 constexpr int kTmaStagesMax = 8;
 constexpr int kTmaConsumerWarps = 8;
 constexpr int kTmaThreads = 32 * (kTmaConsumerWarps + 1);
-constexpr long long kTmaSpinLimit = 1ll << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -42,12 +43,13 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+// One poll that never suspends the thread.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n"
         ".reg .pred p;\n"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         "selp.u32 %0, 1, 0, p;\n"
         "}\n"
         : "=r"(ok)
@@ -56,10 +58,43 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Wait for the phase of `parity` to complete; false (and *err set) after kTmaSpinLimit polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *err, int code) {
-    for (long long it = 0; it < kTmaSpinLimit; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
+// One poll: the thread may be suspended for up to about hint_ns while the phase is incomplete.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity, uint32_t hint_ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for the phase of `parity` to complete; false (and *err set to code) once limit_ns
+// nanoseconds have passed by %globaltimer, or 4 * limit_ns SM cycles by clock64, whichever comes
+// first (the global timer ticks about once a microsecond; the cycle bound makes bounds below its
+// resolution effective and lasts limit_ns or longer at any SM clock up to 4 GHz).  Each round
+// polls once without suspending, checks the bound, then polls with a suspension hinted to at most
+// min(limit_ns, 20 us).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *err, int code,
+                                                  uint64_t limit_ns) {
+    const uint32_t hint = (uint32_t)(limit_ns < 20000ull ? limit_ns : 20000ull);
+    const uint64_t t0 = globaltimer_ns();
+    const long long c0 = clock64();
+    for (;;) {
+        if (mbar_test_wait(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > limit_ns || (uint64_t)(clock64() - c0) > 4ull * limit_ns) break;
+        if (mbar_try_wait(bar, parity, hint)) return true;
+    }
     atomicExch(err, code);
     return false;
 }
@@ -89,7 +124,7 @@ __global__ void __launch_bounds__(kTmaThreads)
     dia_spmv_tma_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
                         const float *__restrict__ aim, int64_t rows, int64_t n_pad, const float *__restrict__ xr,
                         const float *__restrict__ xi, const uint32_t *__restrict__ tmask, int64_t mw, Epi epi,
-                        int *err) {
+                        int *err, uint64_t wait_ns, uint64_t drain_ns) {
     static_assert(G == 4 || G == 8, "4 or 8 states per thread");
     __shared__ DiagMeta sm[kMetaChunk];
     __shared__ uint32_t smk[kMetaChunk];
@@ -122,12 +157,16 @@ __global__ void __launch_bounds__(kTmaThreads)
     if (wid == kTmaConsumerWarps) {  // producer
         if (lane != 0) return;
         int i = 0;
+        // fills i - S .. i - 1 are the last of every stage used: wait until their copies have
+        // landed (a copy in flight always completes; the bound only guards the wait itself)
+        auto drain = [&]() {
+            for (int f = max(i - S, 0); f < i; ++f) mbar_wait_bounded(&full[f % S], (uint32_t)((f / S) & 1), err, 3, drain_ns);
+        };
         for (int j = 0; j < nd; ++j) {
             if (!(smk[j] & bmask)) continue;
             const int s = i % S;
-            if (i >= S && !mbar_wait_bounded(&empty[s], (uint32_t)((i / S - 1) & 1), err, 1)) {
-                for (int f = i - S; f < i; ++f)  // the last fill of every stage
-                    mbar_wait_bounded(&full[f % S], (uint32_t)((f / S) & 1), err, 3);
+            if (i >= S && !mbar_wait_bounded(&empty[s], (uint32_t)((i / S - 1) & 1), err, 1, wait_ns)) {
+                drain();
                 return;
             }
             const DiagMeta m = sm[j];
@@ -149,6 +188,7 @@ __global__ void __launch_bounds__(kTmaThreads)
             }
             ++i;
         }
+        drain();
         return;
     }
 
@@ -163,7 +203,10 @@ __global__ void __launch_bounds__(kTmaThreads)
     for (int j = 0; j < nd; ++j) {
         if (!(smk[j] & bmask)) continue;
         const int s = i % S;
-        if (!mbar_wait_bounded(&full[s], (uint32_t)((i / S) & 1), err, 2)) return;
+        // every lane waits (each must observe the copy's completion); the warp leaves together when
+        // any lane gave up, so no lane is left behind at the __syncwarp below
+        const bool ok = mbar_wait_bounded(&full[s], (uint32_t)((i / S) & 1), err, 2, wait_ns);
+        if (!__all_sync(0xffffffffu, ok)) return;
         const DiagMeta &m = sm[j];
         if (((smk[j] >> tbit) & 1u) && r >= m.lo && r < m.hi) {
             const float *st = stages + s * SF;

@@ -2,6 +2,7 @@
 // spmv_kernel.cuh).  One block per (1024-row word, diagonal): each warp tests four 32-row tiles
 // with a ballot, the block ORs the bits into one word.  Reads every stored value once.
 #include <algorithm>
+#include <vector>
 
 #include "spmv_kernel.cuh"
 
@@ -63,7 +64,7 @@ const uint32_t *cached_tile_mask(const Matrix &A, cudaStream_t s) {
         return nullptr;
     }
     if (A.tmask_ok) return A.tmask;
-    if (!A.tmask && cudaMalloc(&A.tmask, sizeof(uint32_t) * (size_t)A.nd * (size_t)tile_mask_words(A.rows)) != cudaSuccess) {
+    if (!A.tmask && dev_malloc(&A.tmask, sizeof(uint32_t) * (size_t)A.nd * (size_t)tile_mask_words(A.rows)) != cudaSuccess) {
         cudaGetLastError();
         A.tmask = nullptr;
         return nullptr;
@@ -77,3 +78,41 @@ const uint32_t *cached_tile_mask(const Matrix &A, cudaStream_t s) {
 }
 
 }  // namespace diaq_gb300
+
+using namespace diaq_gb300;
+
+extern "C" int diaq_matrix_live_values(diaq_matrix_t A, int64_t *out, void *stream) {
+    if (!A || !out) return set_error(DIAQ_ERR_INVALID, "NULL argument");
+    *out = 0;
+    if (A->nd == 0 || A->rows == 0) return DIAQ_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t W = tile_mask_words(A->rows);
+    uint32_t *mask = nullptr;
+    DQ_CUDA(dev_malloc(&mask, sizeof(uint32_t) * (size_t)A->nd * (size_t)W));
+    std::vector<uint32_t> h((size_t)A->nd * (size_t)W);
+    int st = build_tile_mask(*A, mask, s);
+    cudaError_t e = cudaSuccess;
+    if (st == DIAQ_OK) e = cudaMemcpyAsync(h.data(), mask, sizeof(uint32_t) * h.size(), cudaMemcpyDeviceToHost, s);
+    if (st == DIAQ_OK && e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(mask);
+    if (st != DIAQ_OK) return st;
+    if (e != cudaSuccess) return cuda_status(e, "live values", __FILE__, __LINE__);
+    // every set bit is a 32-row tile with a nonzero: count its stored rows (a tile at either end
+    // of a diagonal holds fewer)
+    int64_t live = 0;
+    for (int j = 0; j < A->nd; ++j) {
+        const DiagMeta &m = A->meta[j];
+        for (int64_t w = 0; w < W; ++w) {
+            uint32_t bits = h[(size_t)j * W + w];
+            while (bits) {
+                const int b = __builtin_ctz(bits);
+                bits &= bits - 1;
+                const int64_t r0 = (w * 32 + b) * 32, r1 = r0 + 32;
+                live += std::max<int64_t>(0, std::min(r1, m.hi) - std::max(r0, m.lo));
+            }
+        }
+    }
+    *out = live;
+    return DIAQ_OK;
+}
+

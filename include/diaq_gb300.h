@@ -91,6 +91,11 @@ int diaq_matrix_info(diaq_matrix_t A, int64_t *rows, int64_t *cols, int32_t *ndi
 /* Copy the offsets (slot order) to a host array of ndiag entries. */
 int diaq_matrix_offsets(diaq_matrix_t A, int32_t *offsets);
 
+/* Stored values that lie in 32-row tiles holding a nonzero (real or imaginary part): the values
+ * the SpMV and time-evolution kernels read, since they skip all-zero tiles -- the figure their
+ * algorithmic bytes are counted from.  Synchronous on stream.  No counterpart in the reference. */
+int diaq_matrix_live_values(diaq_matrix_t A, int64_t *live, void *stream);
+
 /* Packed float64 values to re/im (host arrays, or device arrays when dst_on_device != 0).
  * Replaces deviceDiaQMatrix::to_host (src/deviceMatrix_gpu.cu:97-113). */
 int diaq_matrix_download(diaq_matrix_t A, double *re, double *im, int dst_on_device, void *stream);
@@ -214,6 +219,18 @@ int diaq_expm_negative(diaq_matrix_t A, double t, int max_iterations, double sca
                        double tolerance, int prune, void *stream, diaq_matrix_t *U, int *s_out,
                        int *terms_out);
 
+/* exp(-i t A) as the reference's Pade routine computes it (diaq::expm_negative_pade,
+ * src/spME.cpp:298-445, declared in src/matrixKernels.hpp:86).  A matrix with one diagonal gets
+ * the single-diagonal exponential (exp(t b)(cos(t a) - i sin(t a)) of its values on the main
+ * diagonal of the identity, :309-336); every other input fails as the reference's fails:
+ * rectangular -> DIAQ_ERR_INVALID "addMatrixScaled: matrix shapes do not match"; square with two
+ * or more diagonals -> DIAQ_ERR_UNSUPPORTED "set: diagonal index not present in dIndices." (its
+ * inverse, :521-589, stores the solution into a matrix holding about half the diagonals); square
+ * with none -> DIAQ_ERR_UNSUPPORTED "Matrix is singular, cannot compute inverse." (the reference's
+ * process ends there).  Synchronous. */
+int diaq_expm_negative_pade(diaq_matrix_t A, double t, int max_iterations, double scale_cutoff,
+                            double tolerance, void *stream, diaq_matrix_t *U);
+
 /* exp(A), same method (src/spME.cpp:13-150, src/spME_gpu.cu:10-150). */
 int diaq_expm(diaq_matrix_t A, int max_iterations, double scale_cutoff, double tolerance,
               int prune, void *stream, diaq_matrix_t *U);
@@ -243,15 +260,32 @@ int diaq_evolve_destroy(diaq_evolve_t E);
  * of m Taylor terms.  psi_re/psi_im: float64 device arrays, state q at psi[q*ld ..]; ld must be
  * N.  The first call for a given (dt, s, m, psi) records one step as a CUDA graph; every step is
  * a replay.  A plan keeps up to 16 recorded steps and drops them all when a 17th is needed.
- * dt must be finite.  Asynchronous on stream. */
+ * dt must be finite.  Asynchronous on stream: a bounded wait of the bulk-copy kernels (variants
+ * 10 and 11, chosen only through diaq_evolve_set_config) that gave up during this run is reported
+ * by diaq_evolve_check, or else by the next diaq_evolve_run once the run has finished, as
+ * DIAQ_ERR_TIMEOUT; the states of that run are then not valid. */
 int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld, double dt,
                     int64_t steps, int substeps_log2, int m, void *stream);
 
 /* diaq_evolve_run with host arrays: the nrhs states (state q at psi[q*N ..]) are copied to the
  * device, advanced, and copied back.  Synchronous.  The device copy of the states belongs to the
- * plan: allocated by the first call, reused by the later ones, freed with the plan. */
+ * plan: allocated by the first call, reused by the later ones, freed with the plan.
+ * A wait that gave up during the run is reported by this call (DIAQ_ERR_TIMEOUT). */
 int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
                          int substeps_log2, int m);
+
+/* Wait for the plan's last run on its stream and report whether a bounded wait of a bulk-copy
+ * kernel gave up in it: DIAQ_ERR_TIMEOUT (the error is then cleared), else DIAQ_OK.  No
+ * counterpart in the reference, whose kernels do not wait inside a block. */
+int diaq_evolve_check(diaq_evolve_t E);
+
+/* Time bound, in nanoseconds, of one device-side wait of the bulk-copy kernels (variants 10 and
+ * 11): a consumer warp's wait for a filled shared-memory stage and the producer's wait for a free
+ * one (default 20 ms; 0 restores it).  A wait that runs out records DIAQ_ERR_TIMEOUT for
+ * diaq_evolve_check and its warp leaves; the producer always waits for its copies in flight
+ * (bounded by max(wait, 10 ms)) before its block finishes.  Drops the recorded graphs.  No
+ * counterpart in the reference. */
+int diaq_evolve_set_wait_limit(diaq_evolve_t E, int64_t wait_ns);
 
 /* Launch shape of the plan's term kernel: states per block (1..8: one launch covers every state,
  * in chunks of this many per block, the chunks of a row tile side by side so that the matrix
@@ -263,7 +297,8 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
  * interleaved in tiles of 32 rows x 4 states (any window one aligned vector per lane) and load the
  * matrix 0 / 4 / 8 diagonals ahead into registers; 9 with 8 states per thread; 10 / 11 feed the
  * block's live diagonals through a ring of shared-memory stages filled by bulk asynchronous copies
- * (matrix values and state windows / matrix values only); 12 is 9 with 32-bit row arithmetic and
+ * (matrix values and state windows / matrix values only; never picked by the autotuner, which
+ * measured them slower); 12 is 9 with 32-bit row arithmetic and
  * each diagonal's metadata in one 16-byte shared-memory record (n_pad * states < 2^31).  Every kernel of a
  * plan skips the 32-row tiles of a diagonal that hold only zeros (a mask built from the matrix the
  * plan reads).

@@ -330,3 +330,46 @@ def test_full_size_chosen_form_against_c128(native, mode, model):
     for q in range(8):
         want = out["c128"][q]
         assert np.linalg.norm(out[mode][q] - want) / np.linalg.norm(want) < 1e-6, q
+
+
+@pytest.mark.parametrize("variant", [10, 11])
+def test_bulk_copy_wait_limit_reports_timeout(native, variant):
+    """The bulk-copy kernels' bounded waits: with a 1 ns bound the consumers give up their first
+    wait for a filled stage (a copy takes microseconds).  The run's error comes back as
+    DIAQ_ERR_TIMEOUT from diaq_evolve_check and is cleared; the producer drained its copies, so
+    the same plan with the default bound runs again and matches the oracle."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 14, 8, capi.EVOLVE_HORNER)
+    E.set_config(4, 1, variant)
+    E.set_wait_limit(1)
+    E.run(pr, pi, A.rows, 0.05, 1, 0, 10)
+    with pytest.raises(capi.DiaqError, match="gave up"):
+        E.check()
+    E.check()   # reported once, then cleared
+    E.set_wait_limit(0)
+    import torch
+
+    pr.copy_(torch.from_numpy(np.ascontiguousarray(P.real)))
+    pi.copy_(torch.from_numpy(np.ascontiguousarray(P.imag)))
+    E.run(pr, pi, A.rows, 0.05, 2, 0, 10)
+    E.check()
+    got = _result(pr, pi)
+    for q in (0, 7):
+        want = orc.ham_sim(A, P[q], 0.1, 2, 10)
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, q
+
+
+def test_wait_limit_and_check_on_the_register_kernel(native):
+    """The register kernels have no waits: a 1 ns bound changes nothing and check() stays OK; a
+    negative bound is rejected."""
+    capi, _ = native
+    A, E, P, pr, pi = _setup(capi, 12, 4, capi.EVOLVE_HORNER)
+    E.set_config(4, 1, 12)
+    with pytest.raises(capi.DiaqError):
+        E.set_wait_limit(-1)
+    E.set_wait_limit(1)
+    E.run(pr, pi, A.rows, 0.05, 2, 0, 12)
+    E.check()
+    got = _result(pr, pi)
+    want = orc.ham_sim(A, P[3], 0.1, 2, 12)
+    assert np.linalg.norm(got[3] - want) / np.linalg.norm(want) < 1e-6
