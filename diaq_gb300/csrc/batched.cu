@@ -450,8 +450,8 @@ static int build_items(Batch &B) {
     if (B.d_items) cudaFree(B.d_items);
     if (B.d_il_items) cudaFree(B.d_il_items);
     B.d_items = B.d_il_items = nullptr;
-    DQ_CUDA(cudaMalloc(&B.d_items, sizeof(BatchItem) * std::max<size_t>(items.size(), 1)));
-    DQ_CUDA(cudaMalloc(&B.d_il_items, sizeof(BatchItem) * std::max<size_t>(il_items.size(), 1)));
+    DQ_CUDA(dev_malloc(&B.d_items, sizeof(BatchItem) * std::max<size_t>(items.size(), 1)));
+    DQ_CUDA(dev_malloc(&B.d_il_items, sizeof(BatchItem) * std::max<size_t>(il_items.size(), 1)));
     DQ_CUDA(cudaMemcpy(B.d_items, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice));
     DQ_CUDA(cudaMemcpy(B.d_il_items, il_items.data(), sizeof(BatchItem) * il_items.size(), cudaMemcpyHostToDevice));
     B.n_items = (int)items.size();
@@ -637,7 +637,7 @@ static int autotune(Batch &B) {
     size_t total = 0;
     for (const auto &I : B.inst) total += 2 * (size_t)I.nrhs * (size_t)I.rows;
     double *save = nullptr;
-    DQ_CUDA(cudaMalloc(&save, sizeof(double) * std::max<size_t>(total, 1)));
+    DQ_CUDA(dev_malloc(&save, sizeof(double) * std::max<size_t>(total, 1)));
     size_t o = 0;
     for (const auto &I : B.inst) {
         const size_t c = (size_t)I.nrhs * (size_t)I.rows;
@@ -730,11 +730,11 @@ int diaq_batch_create(int n_inst, const diaq_matrix_t *H, const int *nrhs, doubl
     diaq_batch_s *B = new diaq_batch_s();
     B->prec = prec;
     cudaError_t e = cudaStreamCreateWithFlags(&B->s, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&B->work, work_bytes + 256);
+    if (e == cudaSuccess) e = dev_malloc(&B->work, work_bytes + 256);
     size_t mask_words = 0;
     for (int i = 0; i < n_inst; ++i) mask_words += (size_t)H[i]->nd * (size_t)tile_mask_words(H[i]->rows);
-    if (e == cudaSuccess) e = cudaMalloc(&B->masks, sizeof(uint32_t) * std::max<size_t>(mask_words, 1));
-    if (e == cudaSuccess) e = cudaMalloc(&B->d_inst, sizeof(BatchInst) * n_inst);
+    if (e == cudaSuccess) e = dev_malloc(&B->masks, sizeof(uint32_t) * std::max<size_t>(mask_words, 1));
+    if (e == cudaSuccess) e = dev_malloc(&B->d_inst, sizeof(BatchInst) * n_inst);
     if (e != cudaSuccess) {
         delete B;
         return cuda_status(e, "batch create", __FILE__, __LINE__);

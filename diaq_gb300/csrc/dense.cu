@@ -89,12 +89,12 @@ int from_dense(int64_t rows, int64_t cols, const double *dense, bool on_device, 
     DevBuf staged, flags;
     const double2 *a = reinterpret_cast<const double2 *>(dense);
     if (!on_device) {
-        DQ_CUDA(cudaMalloc(&staged.p, sizeof(double2) * (size_t)n));
+        DQ_CUDA(dev_malloc(&staged.p, sizeof(double2) * (size_t)n));
         DQ_CUDA(cudaMemcpyAsync(staged.p, dense, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice, s));
         a = static_cast<const double2 *>(staged.p);
     }
     const int64_t ndiag = rows + cols - 1;
-    DQ_CUDA(cudaMalloc(&flags.p, sizeof(int) * (size_t)ndiag));
+    DQ_CUDA(dev_malloc(&flags.p, sizeof(int) * (size_t)ndiag));
     DQ_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * (size_t)ndiag, s));
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 16 * num_sms()));
     dense_flags_kernel<<<g, 256, 0, s>>>(a, rows, cols, static_cast<int *>(flags.p));
@@ -140,7 +140,7 @@ int to_dense(const Matrix &A, double *dense, bool on_device, cudaStream_t s) {
     DevBuf staged;
     double2 *a = reinterpret_cast<double2 *>(dense);
     if (!on_device) {
-        DQ_CUDA(cudaMalloc(&staged.p, sizeof(double2) * (size_t)n));
+        DQ_CUDA(dev_malloc(&staged.p, sizeof(double2) * (size_t)n));
         a = static_cast<double2 *>(staged.p);
     }
     DQ_CUDA(cudaMemsetAsync(a, 0, sizeof(double2) * (size_t)n, s));

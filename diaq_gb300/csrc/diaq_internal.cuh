@@ -69,6 +69,25 @@ int cuda_status(cudaError_t e, const char *what, const char *file, int line);
         if (_s != DIAQ_OK) return _s; \
     } while (0)
 
+// ---- device allocation -------------------------------------------------------------------------
+// Every device allocation of the library goes through dev_malloc / dev_malloc_async.  A single
+// allocation larger than the byte count in the environment variable DIAQ_DEVICE_ALLOC_LIMIT
+// (read at every call; unset, empty or unparsable = no limit) fails as cudaErrorMemoryAllocation
+// without reaching the driver, which the entry points report as DIAQ_ERR_OOM: a host-side way to
+// drive the out-of-memory paths (the reference maps a failed cudaMalloc to a runtime error,
+// src/cuda_check.hpp:11-18).
+size_t alloc_limit();
+template <typename T>
+inline cudaError_t dev_malloc(T **p, size_t bytes) {
+    if (bytes > alloc_limit()) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+template <typename T>
+inline cudaError_t dev_malloc_async(T **p, size_t bytes, cudaStream_t s) {
+    if (bytes > alloc_limit()) return cudaErrorMemoryAllocation;
+    return cudaMallocAsync(p, bytes, s);
+}
+
 // ---- geometry ----------------------------------------------------------------------------
 int64_t diag_len(int64_t rows, int64_t cols, int64_t d);
 // Lay out a matrix of these offsets (fills meta, capacity, total); validates the offsets.

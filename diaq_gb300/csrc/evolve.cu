@@ -62,7 +62,7 @@ int diaq_ham_sim(diaq_matrix_t H, const double *psi0_re, const double *psi0_im, 
         return set_error(DIAQ_ERR_INVALID, "hamiltonian_simulation_cuda: vector pointer is NULL");
     cudaStream_t s = (cudaStream_t)stream;
     double *work = nullptr;
-    DQ_CUDA(cudaMallocAsync(&work, sizeof(double) * 6 * (size_t)H->rows, s));
+    DQ_CUDA(dev_malloc_async(&work, sizeof(double) * 6 * (size_t)H->rows, s));
     const int st = ham_sim_run(*H, psi0_re, psi0_im, t, r, max_iterations, psi_re, psi_im, work, s,
                                cached_tile_mask(*H, s));
     cudaError_t e = cudaFreeAsync(work, s);
@@ -84,7 +84,7 @@ int diaq_ham_sim_host(diaq_matrix_t H, const double *psi0_re, const double *psi0
         return set_error(DIAQ_ERR_INVALID, "hamiltonian_simulation_cuda: vector pointer is NULL");
     const int64_t n = H->rows;
     double *buf = nullptr;
-    DQ_CUDA(cudaMalloc(&buf, sizeof(double) * 2 * (size_t)n));
+    DQ_CUDA(dev_malloc(&buf, sizeof(double) * 2 * (size_t)n));
     cudaError_t e = cudaMemcpy(buf, psi0_re, sizeof(double) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(buf + n, psi0_im, sizeof(double) * n, cudaMemcpyHostToDevice);
     int st = e == cudaSuccess ? DIAQ_OK : cuda_status(e, "upload psi0", __FILE__, __LINE__);

@@ -3,6 +3,7 @@
 // and diaQMatrix::pruneMatrix (src/diaQMatrix.hpp:1543-1604).
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <unordered_set>
@@ -29,6 +30,14 @@ int cuda_status(cudaError_t e, const char *what, const char *file, int line) {
         return set_error(DIAQ_ERR_OOM, buf);
     }
     return set_error(DIAQ_ERR_CUDA, buf);
+}
+
+size_t alloc_limit() {
+    const char *v = std::getenv("DIAQ_DEVICE_ALLOC_LIMIT");
+    if (!v || !*v) return SIZE_MAX;
+    char *end = nullptr;
+    const unsigned long long n = std::strtoull(v, &end, 10);
+    return (end && *end == '\0') ? (size_t)n : SIZE_MAX;
 }
 
 int num_sms() {
@@ -101,16 +110,16 @@ int plan_layout(Matrix &M, int64_t rows, int64_t cols, int32_t nd, const int32_t
 int allocate(Matrix &M, cudaStream_t s, bool zero) {
     cudaGetDevice(&M.device);
     const size_t bytes = (size_t)M.capacity * M.elem();
-    DQ_CUDA(cudaMalloc(&M.re, bytes));
-    DQ_CUDA(cudaMalloc(&M.im, bytes));
+    DQ_CUDA(dev_malloc(&M.re, bytes));
+    DQ_CUDA(dev_malloc(&M.im, bytes));
     if (zero) {
         DQ_CUDA(cudaMemsetAsync(M.re, 0, bytes, s));
         DQ_CUDA(cudaMemsetAsync(M.im, 0, bytes, s));
     }
     if (M.nd > 0) {
         // the zero-tile mask's storage, so that SpMV calls never allocate (it is filled on first use)
-        DQ_CUDA(cudaMalloc(&M.tmask, sizeof(uint32_t) * (size_t)M.nd * (size_t)((M.rows + 1023) / 1024)));
-        DQ_CUDA(cudaMalloc(&M.d_meta, sizeof(DiagMeta) * M.nd));
+        DQ_CUDA(dev_malloc(&M.tmask, sizeof(uint32_t) * (size_t)M.nd * (size_t)((M.rows + 1023) / 1024)));
+        DQ_CUDA(dev_malloc(&M.d_meta, sizeof(DiagMeta) * M.nd));
         DQ_CUDA(cudaMemcpyAsync(M.d_meta, M.meta.data(), sizeof(DiagMeta) * M.nd,
                                 cudaMemcpyHostToDevice, s));
         // the host vector may be reallocated later; finish the copy before returning
@@ -328,7 +337,7 @@ int prune_matrix(const Matrix &A, cudaStream_t s, Matrix **out) {
     std::vector<int32_t> flag(A.nd, 1);
     if (A.nd > 0) {
         int32_t *d_flag = nullptr;
-        DQ_CUDA(cudaMalloc(&d_flag, sizeof(int32_t) * A.nd));
+        DQ_CUDA(dev_malloc(&d_flag, sizeof(int32_t) * A.nd));
         const int grid = (int)std::min<int64_t>(A.nd, 65535);
         if (A.prec == DIAQ_C128)
             nonzero_kernel<double><<<grid, 256, 0, s>>>(A.d_meta, A.nd, (const double *)A.re, (const double *)A.im, d_flag);
@@ -351,7 +360,7 @@ int prune_matrix(const Matrix &A, cudaStream_t s, Matrix **out) {
     int st = DIAQ_OK;
     if (C->nd > 0) {
         int32_t *d_map = nullptr;
-        cudaError_t e = cudaMalloc(&d_map, sizeof(int32_t) * C->nd);
+        cudaError_t e = dev_malloc(&d_map, sizeof(int32_t) * C->nd);
         if (e == cudaSuccess) e = cudaMemcpyAsync(d_map, map.data(), sizeof(int32_t) * C->nd, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) st = remap(A, *C, d_map, s);
         else st = cuda_status(e, "prune map", __FILE__, __LINE__);
@@ -394,7 +403,7 @@ int diaq_matrix_create(int64_t rows, int64_t cols, int32_t ndiag, const int32_t 
         int st = DIAQ_OK;
         if (!values_on_device) {
             const size_t bytes = sizeof(double) * (size_t)M->total;
-            cudaError_t e = cudaMalloc(&stage, 2 * bytes);
+            cudaError_t e = dev_malloc(&stage, 2 * bytes);
             if (e == cudaSuccess) e = cudaMemcpyAsync(stage, re, bytes, cudaMemcpyHostToDevice, s);
             if (e == cudaSuccess) e = cudaMemcpyAsync(stage + M->total, im, bytes, cudaMemcpyHostToDevice, s);
             if (e != cudaSuccess) st = cuda_status(e, "upload", __FILE__, __LINE__);
@@ -450,7 +459,7 @@ int diaq_matrix_download(diaq_matrix_t A, double *re, double *im, int dst_on_dev
     }
     double *stage = nullptr;
     const size_t bytes = sizeof(double) * (size_t)A->total;
-    DQ_CUDA(cudaMalloc(&stage, 2 * bytes));
+    DQ_CUDA(dev_malloc(&stage, 2 * bytes));
     int st = gather_packed(*A, stage, stage + A->total, s);
     cudaError_t e = cudaSuccess;
     if (st == DIAQ_OK) e = cudaMemcpyAsync(re, stage, bytes, cudaMemcpyDeviceToHost, s);

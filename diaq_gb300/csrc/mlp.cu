@@ -131,7 +131,7 @@ static int ensure_work(Mlp &M, int B) {
     M.work = nullptr;
     M.cap = 0;
     const size_t per = 6 * kH1 + 2 * kOut + 1;
-    DQ_CUDA(cudaMalloc(&M.work, sizeof(float) * per * (size_t)B));
+    DQ_CUDA(dev_malloc(&M.work, sizeof(float) * per * (size_t)B));
     M.cap = B;
     return DIAQ_OK;
 }
@@ -201,7 +201,7 @@ int diaq_mlp_create(uint64_t seed, diaq_mlp_t *out) {
     init(oW2, kH1, kH1 * kH2);
     init(oW3, kH2, kH2 * kOut);
     diaq_mlp_s *M = new diaq_mlp_s();
-    cudaError_t e = cudaMalloc(&M->p, sizeof(float) * 4 * kParams);
+    cudaError_t e = dev_malloc(&M->p, sizeof(float) * 4 * kParams);
     if (e == cudaSuccess) {
         M->g = M->p + kParams;
         M->m = M->p + 2 * kParams;

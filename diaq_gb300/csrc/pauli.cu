@@ -103,7 +103,7 @@ int pauli_build(int nq, int32_t ns, const double *cre, const double *cim, const 
     const size_t tb = sizeof(PauliTerm) * terms.size(), sb = sizeof(int32_t) * starts.size(),
                  lb = sizeof(int32_t) * list.size();
     uint8_t *d = nullptr;
-    cudaError_t e = cudaMalloc(&d, tb + sb + lb + 64);
+    cudaError_t e = dev_malloc(&d, tb + sb + lb + 64);
     PauliTerm *dt = (PauliTerm *)d;
     int32_t *ds = (int32_t *)(d + tb), *dl = (int32_t *)(d + tb + sb);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dt, terms.data(), tb, cudaMemcpyHostToDevice, s);

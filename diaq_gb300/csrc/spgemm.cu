@@ -119,7 +119,7 @@ int spgemm_symbolic(const Matrix &A, const Matrix &B, std::vector<int32_t> &offC
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     const size_t total = up(fbytes) + up(tbytes) + up(abytes) + up(bbytes) + up(obytes);
     uint8_t *scratch = nullptr;
-    DQ_CUDA(cudaMallocAsync(&scratch, total, s));
+    DQ_CUDA(dev_malloc_async(&scratch, total, s));
     uint8_t *flags = scratch;
     int32_t *tiles = (int32_t *)(scratch + up(fbytes));
     int32_t *dA = (int32_t *)((uint8_t *)tiles + up(tbytes));
@@ -282,7 +282,7 @@ int spgemm_numeric(const Matrix &A, const Matrix &B, Matrix &C, cudaStream_t s) 
                  sbytes = sizeof(int64_t) * ((size_t)C.nd + 1);
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
     uint8_t *scratch = nullptr;
-    DQ_CUDA(cudaMallocAsync(&scratch, up(mbytes) + up(cbytes) + sbytes, s));
+    DQ_CUDA(dev_malloc_async(&scratch, up(mbytes) + up(cbytes) + sbytes, s));
     int32_t *dmap = (int32_t *)scratch;
     int32_t *dcnt = (int32_t *)(scratch + up(mbytes));
     int64_t *dstart = (int64_t *)(scratch + up(mbytes) + up(cbytes));
@@ -302,7 +302,7 @@ int spgemm_numeric(const Matrix &A, const Matrix &B, Matrix &C, cudaStream_t s) 
         for (int32_t c = 0; c < C.nd; ++c) start[(size_t)c + 1] = start[(size_t)c] + cnt[(size_t)c];
         const int64_t npairs = start[(size_t)C.nd];
         e = cudaMemcpyAsync(dstart, start.data(), sbytes, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMallocAsync((void **)&dpairs, sizeof(int2) * (size_t)std::max<int64_t>(npairs, 1), s);
+        if (e == cudaSuccess) e = dev_malloc_async((void **)&dpairs, sizeof(int2) * (size_t)std::max<int64_t>(npairs, 1), s);
     }
     if (e == cudaSuccess) {
         spgemm_pairs_kernel<<<pg, 128, 0, s>>>(A.d_meta, A.nd, B.d_meta, dmap, bmin, bmax, C.d_meta, C.nd, nullptr,

@@ -112,7 +112,7 @@ int diaq_spmv_host(diaq_matrix_t A, const double *x_re, const double *x_im, doub
     if (!x_re || !x_im || !y_re || !y_im) return set_error(DIAQ_ERR_INVALID, "vector pointer is NULL");
     Scratch w;
     const int64_t M = A->rows, N = A->cols;
-    DQ_CUDA(cudaMalloc(&w.p, sizeof(double) * (size_t)(2 * N + 2 * M)));
+    DQ_CUDA(dev_malloc(&w.p, sizeof(double) * (size_t)(2 * N + 2 * M)));
     double *xr = w.p, *xi = w.p + N, *yr = w.p + 2 * N, *yi = w.p + 2 * N + M;
     DQ_CUDA(cudaMemcpy(xr, x_re, sizeof(double) * N, cudaMemcpyHostToDevice));
     DQ_CUDA(cudaMemcpy(xi, x_im, sizeof(double) * N, cudaMemcpyHostToDevice));
@@ -142,7 +142,7 @@ int diaq_spmv_ntimes_host(diaq_matrix_t A, const double *x_re, const double *x_i
     if (M == 0) return DIAQ_OK;
     Scratch w;
     const int64_t L = std::max(M, N);
-    DQ_CUDA(cudaMalloc(&w.p, sizeof(double) * (size_t)(4 * L)));
+    DQ_CUDA(dev_malloc(&w.p, sizeof(double) * (size_t)(4 * L)));
     double *ar = w.p, *ai = w.p + L, *br = w.p + 2 * L, *bi = w.p + 3 * L;
     DQ_CUDA(cudaMemcpy(ar, x_re, sizeof(double) * N, cudaMemcpyHostToDevice));
     DQ_CUDA(cudaMemcpy(ai, x_im, sizeof(double) * N, cudaMemcpyHostToDevice));

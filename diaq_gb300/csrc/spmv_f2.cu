@@ -267,7 +267,7 @@ int f2_spmv(const Matrix &A, const double *xr, const double *xi, double *yr, dou
     const int64_t n = A.cols;
     const int64_t np = (n + 31) / 32 * 32;  // planes 128-byte aligned: equal alignment for hi and lo
     float *buf = nullptr;
-    DQ_CUDA(cudaMallocAsync(&buf, sizeof(float) * 4 * (size_t)std::max<int64_t>(np, 32), s));
+    DQ_CUDA(dev_malloc_async(&buf, sizeof(float) * 4 * (size_t)std::max<int64_t>(np, 32), s));
     float *xrh = buf, *xrl = buf + np, *xih = buf + 2 * np, *xil = buf + 3 * np;
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * num_sms()));
     const int vec = ((uintptr_t)xr % 16 == 0) && ((uintptr_t)xi % 16 == 0);
