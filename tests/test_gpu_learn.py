@@ -2,7 +2,6 @@
 network trained by the project's kernels proposes, every proposal is checked, and the checked
 choice is never less accurate and never dearer than the norm-bound selection -- and cheaper
 on average, which is the gain the network brings."""
-import math
 
 import numpy as np
 import pytest
@@ -18,7 +17,7 @@ def test_labels_meet_tolerance(native):
         n, terms, t, tol = learn.random_instance(rng, 8, 10)
         r = learn.instance_record(n, terms, t, tol, seed=int(rng.integers(1 << 30)))
         s, m, cost = r["label"]
-        assert learn._error(r["U"], t, s, m, r["norm1"]) <= tol
+        assert learn._error(r, t, s, m) <= tol
         s_ref, m_ref = r["ref"]
         assert cost <= 2 ** s_ref * m_ref
         assert r["f"].shape == (16,) and np.all(np.isfinite(r["f"]))
@@ -56,8 +55,7 @@ def test_trained_selector_gains_over_norm_bound(native):
     rows = learn.evaluate(net, 25, seed=99, n_lo=10, n_hi=11)
     for r in rows:
         assert r["cost"] <= r["cost_ref"]
-        if not math.isnan(r["err"]):
-            assert r["err"] <= r["tol"]
+        assert r["err"] <= r["tol"], r   # every row: the chain's tail, or direct evolution beyond its reach
     gain = np.mean([r["cost_ref"] / r["cost"] for r in rows])
     assert gain > 1.0, gain
 
@@ -79,3 +77,34 @@ def test_selection_streams_the_chain(native):
         net = learn.load()
         if net is not None:
             assert learn.choose(net, lean, t, tol) == learn.choose(net, full, t, tol)
+
+
+def test_evolve_error_beyond_the_chain(native):
+    """Where tau ||H||_1 > 8 the chain cannot give the truncation error; the direct evolution does,
+    and inside the chain's reach the two agree."""
+    from diaq_gb300 import learn
+
+    rng = np.random.default_rng(5)
+    n, terms, _, _ = learn.random_instance(rng, 9, 9)
+    H = learn.build(n, terms)
+    rec = learn.record_for(H, n, 0.05, 1e-10, seed=3, with_label=True)
+    t = 2.0 / rec["norm1"]    # tau ||H||_1 = 2: inside the chain's reach
+    for s, m in ((0, 8), (1, 6), (0, 14)):
+        e_chain = learn._error(rec, t, s, m)
+        e_direct = learn.evolve_error(H, rec["U"][0], t, s, m, rec["norm1"])
+        assert abs(e_chain - e_direct) <= 1e-12 + 1e-6 * e_chain, (s, m, e_chain, e_direct)
+    # tau ||H||_1 = 12 at s = 0: beyond the chain's reach, the direct evolution takes over; check
+    # it against the degree-m Taylor step of the oracle and a dense exp(-i t H) (scipy)
+    import scipy.linalg as sl
+
+    from oracle import oracle as orc
+
+    t = 12.0 / rec["norm1"]
+    off, re, im = H.download()
+    A = orc.OMatrix(1 << n, 1 << n, off, re, im)
+    psi = rec["U"][0].cpu().numpy()
+    exact = sl.expm(-1j * t * A.to_dense()) @ psi
+    for s, m in ((0, 14), (0, 30), (0, 22)):   # all beyond the chain: direct evolution
+        e = learn._error(rec, t, s, m)
+        want = np.linalg.norm(orc.ham_sim(A, psi, t, 1, m, substeps=1 << s) - exact)
+        assert abs(e - want) <= 1e-13 + 1e-6 * want, (s, m, e, want)
