@@ -29,6 +29,7 @@ __device__ __forceinline__ int64_t il_at(int64_t r, int quad, int quads) {
 // One Taylor term's epilogue for four interleaved states of one row: the compensated forward sum
 // (the arithmetic of the planar EpiMixed of the evolution plans).
 struct EpiMixedIL {
+    static constexpr bool kPsiTile = false;
     float *vr, *vi;                 // term out (interleaved)
     float *hr, *hi_, *lr, *li;      // compensated sum (interleaved)
     double *pr, *pi;                // state, q at p[q * ld + r]
@@ -103,6 +104,25 @@ struct EpiHornerIL {
     int sp, nrhs;
     float scale;
     int last;
+    // A middle step reads one fp32(psi) quad per plane and row: kernels may fetch it ahead into
+    // shared memory and hand it to apply_psi.
+    static constexpr bool kPsiTile = true;
+    __device__ __forceinline__ bool reads_psi() const { return !last; }
+    __device__ __forceinline__ void apply_psi(int64_t r, int g, const float (&sr)[4], const float (&si)[4],
+                                              const float4 &a, const float4 &b) const {
+        const int64_t i = il_at(r, g, sp >> 2);
+        float tr[4], ti[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tr[c] = si[c] * scale;
+            ti[c] = -sr[c] * scale;
+        }
+        // unfused (rounded product, then rounded sum): the planar kernels give the same bits
+        *reinterpret_cast<float4 *>(wr + i) = make_float4(__fadd_rn(a.x, tr[0]), __fadd_rn(a.y, tr[1]),
+                                                          __fadd_rn(a.z, tr[2]), __fadd_rn(a.w, tr[3]));
+        *reinterpret_cast<float4 *>(wi + i) = make_float4(__fadd_rn(b.x, ti[0]), __fadd_rn(b.y, ti[1]),
+                                                          __fadd_rn(b.z, ti[2]), __fadd_rn(b.w, ti[3]));
+    }
     __device__ __forceinline__ void apply(int64_t r, int g, const float (&sr)[4], const float (&si)[4]) const {
         const int64_t i = il_at(r, g, sp >> 2);
         float tr[4], ti[4];
@@ -113,11 +133,7 @@ struct EpiHornerIL {
         }
         if (!last) {
             const float4 a = *reinterpret_cast<const float4 *>(fr + i), b = *reinterpret_cast<const float4 *>(fi + i);
-            // unfused (rounded product, then rounded sum): the planar kernels give the same bits
-            *reinterpret_cast<float4 *>(wr + i) = make_float4(__fadd_rn(a.x, tr[0]), __fadd_rn(a.y, tr[1]),
-                                                              __fadd_rn(a.z, tr[2]), __fadd_rn(a.w, tr[3]));
-            *reinterpret_cast<float4 *>(wi + i) = make_float4(__fadd_rn(b.x, ti[0]), __fadd_rn(b.y, ti[1]),
-                                                              __fadd_rn(b.z, ti[2]), __fadd_rn(b.w, ti[3]));
+            apply_psi(r, g, sr, si, a, b);
         } else {
             float nr_[4], ni_[4];
 #pragma unroll
