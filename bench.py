@@ -35,7 +35,7 @@ METRIC = "expm(-iHt)·ψ states·steps/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the chosen form's term kernel,
 # from ncu captures (profiles/), keyed by (qubits, states, form, states per block, rows per thread,
 # variant); the kernels skip all-zero 32-row tiles
-TRAFFIC_PER_LAUNCH = {(20, 8, "horner", 4, 1, 9): 390.6e6, (20, 8, "horner", 4, 1, 12): 387.0e6}
+TRAFFIC_PER_LAUNCH = {(20, 8, "horner", 4, 1, 9): 390.6e6, (20, 8, "horner", 4, 1, 12): 363.8e6}
 
 
 def peaks():
