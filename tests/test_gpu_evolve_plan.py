@@ -373,3 +373,43 @@ def test_wait_limit_and_check_on_the_register_kernel(native):
     got = _result(pr, pi)
     want = orc.ham_sim(A, P[3], 0.1, 2, 12)
     assert np.linalg.norm(got[3] - want) / np.linalg.norm(want) < 1e-6
+
+
+@pytest.mark.parametrize("N,k", [(1500, 8), (2048 + 96, 8), (3000, 5), (777, 16)])
+def test_horner_il32_ragged_sizes(native, N, k):
+    """The bench line's kernel (variant 12) on row counts that are not powers of two: the last
+    32-row tile padded, grids that the block swizzle maps (a multiple of 4 blocks) and that it
+    leaves in order (not), and the fp32(psi) tile of rows past the end skipped -- against the
+    oracle, on a random Hermitian matrix with near, far and unaligned offsets."""
+    import torch
+
+    capi, _ = native
+    rng = np.random.default_rng(N)
+    offs = sorted({0, 1, 3, 32, 100, N // 3, N - 5})
+    off, re, im = [], [], []
+    for d in offs:
+        L = N - d
+        a = rng.standard_normal(L) + 1j * rng.standard_normal(L)
+        if d == 0:
+            a = a.real + 0j
+        a[rng.random(L) < 0.4] = 0          # zero runs: some 32-row tiles hold only zeros
+        for dd, v in ((d, a), (-d, np.conj(a))) if d else ((0, a),):
+            off.append(dd)
+            re.append(v.real * 0.3)
+            im.append(v.imag * 0.3)
+    order = np.argsort(off)
+    off = np.asarray(off, dtype=np.int32)[order]
+    re = np.concatenate([re[i] for i in order])
+    im = np.concatenate([im[i] for i in order])
+    H = capi.Matrix.create(N, N, off, re, im)
+    E = capi.Evolve(H, k, capi.EVOLVE_HORNER)
+    E.set_config(4, 1, 12)
+    P = ham.random_state(N, 3, k=k)
+    pr = torch.from_numpy(np.ascontiguousarray(P.real)).cuda()
+    pi = torch.from_numpy(np.ascontiguousarray(P.imag)).cuda()
+    E.run(pr, pi, N, 0.02, 3, 0, 12)
+    got = _result(pr, pi)
+    A = orc.OMatrix(N, N, off, re, im)
+    for q in (0, k - 1):
+        want = orc.ham_sim(A, P[q], 0.06, 3, 12)
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, q
