@@ -120,3 +120,29 @@ def test_other_operations_refuse(native):
         M.prune()
     with pytest.raises(capi.DiaqError):
         capi.Evolve(M, 1)
+
+
+@pytest.mark.parametrize("lo_exp,hi_exp", [(-6, 6), (-28, -20), (20, 36), (-28, 36)])
+def test_x_over_the_split_ranges(native, lo_exp, hi_exp):
+    """x spread over decades that the split of x into float pairs handles with bit operations
+    (|x| in about 1e-22 .. 3e38) and with the IEEE fallback below that, zeros included: every
+    element of the float-pair SpMV within 1e-12 of the float64 oracle, relative to |A| |x| of its
+    row (the products' own scale: x spans many decades within one vector)."""
+    capi, _ = native
+    rng = np.random.default_rng(lo_exp + 100)
+    N = 2048
+    off = [0, 1, -3]
+    lens = [N, N - 1, N - 3]
+    re = np.concatenate([rng.uniform(0.5, 1.5, n) for n in lens])
+    im = np.concatenate([rng.uniform(-0.5, 0.5, n) for n in lens])
+    A = orc.OMatrix(N, N, off, re, im)
+    A_abs = orc.OMatrix(N, N, off, np.hypot(re, im), np.zeros_like(im))
+    mag = 10.0 ** rng.uniform(lo_exp, hi_exp, N)
+    x = (rng.standard_normal(N) + 1j * rng.standard_normal(N)) * mag
+    x[::97] = 0
+    got = _spmv_capi(capi, A, x, precision=F2)
+    want = orc.spmv(A, x)
+    scale = orc.spmv(A_abs, np.abs(x)).real
+    ok = scale > 0
+    assert np.all(np.abs(got - want)[ok] <= 1e-12 * scale[ok])
+    assert np.all(got[~ok] == 0)
