@@ -1109,12 +1109,14 @@ def run_ours(args, rank, world):
     achieved = step_bytes / (ms / K * 1e-3) / 1e9
     k_launch, v_launch = chosen.config()
     variant = chosen.pipelined()
-    il_names = {6: "dia_spmv_il_kernel<EpiHornerIL,0,4>", 7: "dia_spmv_il_kernel<EpiHornerIL,4,4>",
-                8: "dia_spmv_il_kernel<EpiHornerIL,8,4>", 9: "dia_spmv_il_kernel<EpiHornerIL,0,8>",
-                10: "dia_spmv_tma_kernel<EpiHornerIL,8,true,4>", 11: "dia_spmv_tma_kernel<EpiHornerIL,8,false,8>",
-                12: "dia_spmv_il32_kernel<EpiHornerIL,8,5>"}
+    # EpiHorner*<0/1>: the middle terms' and the last term's instantiations of one kernel
+    il_names = {6: "dia_spmv_il_kernel<EpiHornerT<0/1>,0,4>", 7: "dia_spmv_il_kernel<EpiHornerT<0/1>,4,4>",
+                8: "dia_spmv_il_kernel<EpiHornerT<0/1>,8,4>", 9: "dia_spmv_il_kernel<EpiHornerT<0/1>,0,8>",
+                10: "dia_spmv_tma_kernel<EpiHornerT<0/1>,8,true,4>",
+                11: "dia_spmv_tma_kernel<EpiHornerT<0/1>,8,false,8>",
+                12: "dia_spmv_il32_kernel<EpiHornerT<0/1>,8,5>"}
     kernel = (il_names.get(variant) if variant >= 6 else
-              f"dia_spmv_kernel<float,{k_launch},{v_launch},EpiHorner>" if variant == 0 else
+              f"dia_spmv_kernel<float,{k_launch},{v_launch},EpiHornerP<0/1>>" if variant == 0 else
               f"variant {variant}, {k_launch} states x {v_launch} rows per thread")
     # DRAM bytes of one launch from the ncu capture of this workload, form and shape (profiles/);
     # null for shapes not captured

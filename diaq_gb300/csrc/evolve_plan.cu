@@ -160,7 +160,10 @@ struct EpiMixed {
 // One Horner step: w_out = fp32(psi) + (-i * scale) (A w_in); on the outermost step (last)
 // psi += (-i * scale) (A w_1) in float64 and the fresh fp32(psi) goes to g (which is not the
 // fp32(psi) this launch reads when the step's SpMV also reads it, m = 1).
-struct EpiHorner {
+// LAST = 0 / 1: a middle / the last step fixed at compile time (the kernels of middle steps then
+// carry no float64 code); -1: the runtime field `last` decides.
+template <int LAST = -1>
+struct EpiHornerP {
     float *wr, *wi;                 // w out
     const float *fr, *fi;           // fp32(psi)
     double *pr, *pi;                // psi
@@ -168,8 +171,9 @@ struct EpiHorner {
     int64_t ld;
     float scale;
     int last;
-    __host__ __device__ EpiHorner shifted(int q0) const {
-        EpiHorner e = *this;
+    __host__ __device__ __forceinline__ bool is_last() const { return LAST < 0 ? last != 0 : LAST == 1; }
+    __host__ __device__ EpiHornerP shifted(int q0) const {
+        EpiHornerP e = *this;
         const int64_t o = q0 * ld;
         e.wr += o;
         e.wi += o;
@@ -191,7 +195,7 @@ struct EpiHorner {
                 if (q >= kq || r >= rows) continue;
                 const int64_t i = q * ld + r;
                 const float tr = si[q][v] * scale, ti = -sr[q][v] * scale;
-                if (!last) {
+                if (!is_last()) {
                     wr[i] = __fadd_rn(fr[i], tr);  // unfused, as the interleaved epilogue
                     wi[i] = __fadd_rn(fi[i], ti);
                 } else {
@@ -391,6 +395,30 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // - When the block count is a multiple of 4, consecutive blocks take row blocks b, b + B/4,
 //   b + B/2, b + 3B/4 (B blocks): the blocks resident together spread over four distant parts of
 //   the rows (-2 %).
+// - While staging the metadata, the thread of each diagonal asks L2 for that diagonal's values in
+//   the block's live tiles (bulk prefetches, one per run of live tiles and plane), and thread 0
+//   for the block's own rows of the input states: the warps' matrix loads of the later diagonals
+//   then hit L2 (104.6 -> 100.1 us per 8-state term; 201 -> 178 us for 16 states).  Asking for
+//   the tiles of the block that launches one resident wave later instead made it slower (117 us).
+// Asks L2 for the values one diagonal holds in a block's rows: one bulk prefetch per plane and
+// run of live 32-row tiles among the block's T tiles from row row0 (mask bits `bits`, bit j =
+// tile j), clipped to the stored rows [lo, hi) widened to whole tiles.  Tile starts are 128-byte
+// aligned in every c64 plane (base is a multiple of 32 values), and the widened ends stay inside
+// the allocation (a guard of 32 values before the first diagonal and after the last).
+__device__ __forceinline__ void prefetch_tiles_l2(const float *are, const float *aim, int64_t base, int lo, int hi,
+                                                  uint32_t bits, int row0) {
+    while (bits) {
+        const int j = __ffs(bits) - 1;
+        const int len = __ffs(~(bits >> j)) - 1;   // live tiles j .. j + len - 1
+        bits &= ~(((1u << len) - 1u) << j);
+        const int a = max(row0 + 32 * j, lo & ~31), b = min(row0 + 32 * (j + len), (hi + 31) & ~31);
+        if (a >= b) continue;
+        const uint32_t bytes = (uint32_t)(b - a) * 4u;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(are + base + a), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(aim + base + a), "r"(bytes) : "memory");
+    }
+}
+
 template <class Epi, int G, int MINB>
 __global__ void __launch_bounds__(kSpmvThreads, MINB)
     dia_spmv_il32_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
@@ -430,6 +458,15 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
+    if (threadIdx.x == 0 && row0 < rows) {
+        // the block's own rows of the input states (all quads: one contiguous run per plane),
+        // inside the rows padded to 32
+        const int64_t at = (int64_t)(row0 >> 5) * quads * 128;
+        const int tiles = min(8 / groups, (rows + 31 - row0) >> 5);
+        const uint32_t bytes = (uint32_t)tiles * (uint32_t)quads * 512u;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(xr + at), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(xi + at), "r"(bytes) : "memory");
+    }
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, nd - c0);
         __syncthreads();
@@ -438,6 +475,9 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
             const uint32_t w = tmask ? tmask[(int64_t)(c0 + i) * mw + (row0 >> 10)] : 0xffffffffu;
             sq[i] = make_int4(m.off, (int)m.lo, (int)m.hi, (int)w);
             sb[i] = m.base;
+            const int T = 8 / groups;   // the block's tiles, inside one mask word
+            prefetch_tiles_l2(are, aim, m.base, (int)m.lo, (int)m.hi, (w >> ((row0 >> 5) & 31)) & ((1u << T) - 1u),
+                              row0);
         }
         __syncthreads();
         if (r >= rows) continue;
@@ -631,8 +671,9 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
     if (e == cudaSuccess && bytes) e = dev_malloc(&P->buf, bytes);
     if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
     if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
-    if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128)
-        st = mode == DIAQ_EVOLVE_HORNER ? allow_tma_smem<EpiHornerIL>() : allow_tma_smem<EpiMixedIL>();
+    if (st == DIAQ_OK && mode == DIAQ_EVOLVE_MIXED) st = allow_tma_smem<EpiMixedIL>();
+    if (st == DIAQ_OK && mode == DIAQ_EVOLVE_HORNER) st = allow_tma_smem<EpiHornerT<0>>();
+    if (st == DIAQ_OK && mode == DIAQ_EVOLVE_HORNER) st = allow_tma_smem<EpiHornerT<1>>();
     if (st == DIAQ_OK) {
         e = dev_malloc(&P->err, sizeof(int));
         if (e == cudaSuccess) e = cudaMemsetAsync(P->err, 0, sizeof(int), P->s);
@@ -736,13 +777,23 @@ static int enqueue_step(EvolvePlan &P, double dt, int sl, int m, double *pr, dou
                 // the last step refreshes fp32(psi); when it also reads fp32(psi) (m = 1) it writes
                 // the fresh copy to the free w vector, copied back after the launch
                 float *gr = (last && in_r == fr) ? out_r : fr, *gi = (last && in_r == fr) ? out_i : fi;
+                // middle and last steps are separate kernel instantiations (EpiHorner*<0> / <1>)
                 if (P.interleaved()) {
-                    EpiHornerIL e{out_r, out_i, fr, fi, gr, gi, pr, pi, ld, P.sp, (int)k, scale, last};
-                    DQ_TRY(launch_il(P, in_r, in_i, e));
+                    if (last) {
+                        EpiHornerT<1> e{out_r, out_i, fr, fi, gr, gi, pr, pi, ld, P.sp, (int)k, scale, 1};
+                        DQ_TRY(launch_il(P, in_r, in_i, e));
+                    } else {
+                        EpiHornerT<0> e{out_r, out_i, fr, fi, gr, gi, pr, pi, ld, P.sp, (int)k, scale, 0};
+                        DQ_TRY(launch_il(P, in_r, in_i, e));
+                    }
+                } else if (last) {
+                    EpiHornerP<1> e{out_r, out_i, fr, fi, pr, pi, gr, gi, L, scale, 1};
+                    DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiHornerP<1>, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e,
+                                                                                P.s, P.cfg, P.tmask)));
                 } else {
-                    EpiHorner e{out_r, out_i, fr, fi, pr, pi, gr, gi, L, scale, last};
-                    DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiHorner, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e, P.s,
-                                                                            P.cfg, P.tmask)));
+                    EpiHornerP<0> e{out_r, out_i, fr, fi, pr, pi, gr, gi, L, scale, 0};
+                    DQ_TRY((launch_dia_spmv_rhs_cfg<float, EpiHornerP<0>, 4, 2, 1>(*P.Hc, in_r, in_i, L, (int)k, e,
+                                                                                P.s, P.cfg, P.tmask)));
                 }
                 ++P.launches_per_step;
                 if (gr != fr) {

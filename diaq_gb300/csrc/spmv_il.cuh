@@ -94,8 +94,11 @@ struct EpiMixedIL {
     }
 };
 
-// The Horner step (EpiHorner) for four interleaved states of one row.
-struct EpiHornerIL {
+// The Horner step (EpiHorner) for four interleaved states of one row.  LAST = 0 / 1 fixes at compile
+// time whether this is a middle or the last step (-1: the runtime field `last` says), so that a
+// middle step's kernel carries none of the last step's float64 code.
+template <int LAST = -1>
+struct EpiHornerT {
     float *wr, *wi;                 // interleaved: w out
     const float *fr, *fi;           // fp32(psi)
     float *gr, *gi;                 // fp32(psi) written on the last step
@@ -107,7 +110,8 @@ struct EpiHornerIL {
     // A middle step reads one fp32(psi) quad per plane and row: kernels may fetch it ahead into
     // shared memory and hand it to apply_psi.
     static constexpr bool kPsiTile = true;
-    __device__ __forceinline__ bool reads_psi() const { return !last; }
+    __host__ __device__ __forceinline__ bool is_last() const { return LAST < 0 ? last != 0 : LAST == 1; }
+    __device__ __forceinline__ bool reads_psi() const { return !is_last(); }
     __device__ __forceinline__ void apply_psi(int64_t r, int g, const float (&sr)[4], const float (&si)[4],
                                               const float4 &a, const float4 &b) const {
         const int64_t i = il_at(r, g, sp >> 2);
@@ -131,7 +135,7 @@ struct EpiHornerIL {
             tr[c] = si[c] * scale;
             ti[c] = -sr[c] * scale;
         }
-        if (!last) {
+        if (!is_last()) {
             const float4 a = *reinterpret_cast<const float4 *>(fr + i), b = *reinterpret_cast<const float4 *>(fi + i);
             apply_psi(r, g, sr, si, a, b);
         } else {
@@ -153,6 +157,7 @@ struct EpiHornerIL {
         }
     }
 };
+using EpiHornerIL = EpiHornerT<-1>;
 
 // The state window of G states (G / 4 quads from quad g0) at column c: two 16-byte loads per quad.
 template <int G>
