@@ -400,25 +400,6 @@ __global__ void __launch_bounds__(kSpmvThreads)
 //   for the block's own rows of the input states: the warps' matrix loads of the later diagonals
 //   then hit L2 (104.6 -> 100.1 us per 8-state term; 201 -> 178 us for 16 states).  Asking for
 //   the tiles of the block that launches one resident wave later instead made it slower (117 us).
-// Asks L2 for the values one diagonal holds in a block's rows: one bulk prefetch per plane and
-// run of live 32-row tiles among the block's T tiles from row row0 (mask bits `bits`, bit j =
-// tile j), clipped to the stored rows [lo, hi) widened to whole tiles.  Tile starts are 128-byte
-// aligned in every c64 plane (base is a multiple of 32 values), and the widened ends stay inside
-// the allocation (a guard of 32 values before the first diagonal and after the last).
-__device__ __forceinline__ void prefetch_tiles_l2(const float *are, const float *aim, int64_t base, int lo, int hi,
-                                                  uint32_t bits, int row0) {
-    while (bits) {
-        const int j = __ffs(bits) - 1;
-        const int len = __ffs(~(bits >> j)) - 1;   // live tiles j .. j + len - 1
-        bits &= ~(((1u << len) - 1u) << j);
-        const int a = max(row0 + 32 * j, lo & ~31), b = min(row0 + 32 * (j + len), (hi + 31) & ~31);
-        if (a >= b) continue;
-        const uint32_t bytes = (uint32_t)(b - a) * 4u;
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(are + base + a), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(aim + base + a), "r"(bytes) : "memory");
-    }
-}
-
 template <class Epi, int G, int MINB>
 __global__ void __launch_bounds__(kSpmvThreads, MINB)
     dia_spmv_il32_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
@@ -475,9 +456,8 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
             const uint32_t w = tmask ? tmask[(int64_t)(c0 + i) * mw + (row0 >> 10)] : 0xffffffffu;
             sq[i] = make_int4(m.off, (int)m.lo, (int)m.hi, (int)w);
             sb[i] = m.base;
-            const int T = 8 / groups;   // the block's tiles, inside one mask word
-            prefetch_tiles_l2(are, aim, m.base, (int)m.lo, (int)m.hi, (w >> ((row0 >> 5) & 31)) & ((1u << T) - 1u),
-                              row0);
+            // the block's tiles, inside one mask word
+            prefetch_tiles_l2(are, aim, m.base, m.lo, m.hi, block_tile_bits(w, row0, 8 / groups), row0);
         }
         __syncthreads();
         if (r >= rows) continue;

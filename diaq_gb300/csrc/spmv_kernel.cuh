@@ -102,6 +102,37 @@ __device__ __forceinline__ bool aligned_to(const void *p) {
 }
 __device__ __forceinline__ bool aligned16(const void *p) { return aligned_to<16>(p); }
 
+// Asks L2 for the values one diagonal holds in a block's rows: one bulk prefetch per plane and
+// run of live 32-row tiles among the block's tiles from row row0 (mask bits `bits`, bit j = tile
+// j), clipped to the stored rows [lo, hi) widened to whole tiles.  Tile starts are 128-byte
+// aligned in every plane (base is a multiple of 32 values), and the widened ends stay inside the
+// allocation (a guard of 32 values before the first diagonal and after the last).  The
+// interleaved kernels (256 rows per block) use it; in the planar kernel below and the float-pair
+// SpMV (1,024 rows per block, up to 8 KB per diagonal and plane ahead) it measured slower on the
+// 20-qubit chain -- one-state Horner evolution 2,106 -> 1,693 states x steps/s, float-pair SpMV
+// 99 -> 132 us -- and is not called there.
+template <typename T>
+__device__ __forceinline__ void prefetch_tiles_l2(const T *are, const T *aim, int64_t base, int64_t lo, int64_t hi,
+                                                  uint32_t bits, int64_t row0) {
+    while (bits) {
+        const int j = __ffs(bits) - 1;
+        const uint32_t run = bits >> j;
+        const int len = run == 0xffffffffu ? 32 : __ffs(~run) - 1;   // live tiles j .. j + len - 1
+        bits = len + j >= 32 ? 0u : bits & ~(((1u << len) - 1u) << j);
+        const int64_t a = max(row0 + 32 * j, lo & ~(int64_t)31);
+        const int64_t b = min(row0 + 32 * (int64_t)(j + len), (hi + 31) & ~(int64_t)31);
+        if (a >= b) continue;
+        const uint32_t bytes = (uint32_t)(b - a) * (uint32_t)sizeof(T);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(are + base + a), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(aim + base + a), "r"(bytes) : "memory");
+    }
+}
+
+// Mask bits of the `tiles` (1 .. 32) tiles from row row0 in the 1024-row mask word w.
+__device__ __forceinline__ uint32_t block_tile_bits(uint32_t w, int64_t row0, int tiles) {
+    return tiles >= 32 ? w : (w >> ((row0 >> 5) & 31)) & ((1u << tiles) - 1u);
+}
+
 // nrhs states in nchunk chunks of up to K, VR rows per thread.  Block b works on chunk
 // b % nchunk of row tile b / nchunk: the blocks of one row tile are neighbours in launch order and
 // run at the same time, so the matrix tile they all read comes from HBM once and from L2 for the
