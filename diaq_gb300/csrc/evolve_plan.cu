@@ -399,7 +399,8 @@ __global__ void __launch_bounds__(kSpmvThreads)
 //   the block's live tiles (bulk prefetches, one per run of live tiles and plane), and thread 0
 //   for the block's own rows of the input states: the warps' matrix loads of the later diagonals
 //   then hit L2 (104.6 -> 100.1 us per 8-state term; 201 -> 178 us for 16 states).  Asking for
-//   the tiles of the block that launches one resident wave later instead made it slower (117 us).
+//   the tiles of the block that launches one resident wave later instead made it slower (117 us),
+//   and so did asking, with each live run, for the state windows it reads (111 us).
 template <class Epi, int G, int MINB>
 __global__ void __launch_bounds__(kSpmvThreads, MINB)
     dia_spmv_il32_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
@@ -445,8 +446,8 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
         const int64_t at = (int64_t)(row0 >> 5) * quads * 128;
         const int tiles = min(8 / groups, (rows + 31 - row0) >> 5);
         const uint32_t bytes = (uint32_t)tiles * (uint32_t)quads * 512u;
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(xr + at), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(xi + at), "r"(bytes) : "memory");
+        prefetch_l2(xr + at, bytes);
+        prefetch_l2(xi + at, bytes);
     }
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, nd - c0);

@@ -110,10 +110,9 @@ __device__ __forceinline__ bool aligned16(const void *p) { return aligned_to<16>
 // interleaved kernels (256 rows per block) use it; in the planar kernel below and the float-pair
 // SpMV (1,024 rows per block, up to 8 KB per diagonal and plane ahead) it measured slower on the
 // 20-qubit chain -- one-state Horner evolution 2,106 -> 1,693 states x steps/s, float-pair SpMV
-// 99 -> 132 us -- and is not called there.
-template <typename T>
-__device__ __forceinline__ void prefetch_tiles_l2(const T *are, const T *aim, int64_t base, int64_t lo, int64_t hi,
-                                                  uint32_t bits, int64_t row0) {
+// 99 -> 132 us -- and is not called there.  for_live_runs calls f(a, b) for each such run of rows.
+template <class F>
+__device__ __forceinline__ void for_live_runs(uint32_t bits, int64_t row0, int64_t lo, int64_t hi, F &&f) {
     while (bits) {
         const int j = __ffs(bits) - 1;
         const uint32_t run = bits >> j;
@@ -121,11 +120,20 @@ __device__ __forceinline__ void prefetch_tiles_l2(const T *are, const T *aim, in
         bits = len + j >= 32 ? 0u : bits & ~(((1u << len) - 1u) << j);
         const int64_t a = max(row0 + 32 * j, lo & ~(int64_t)31);
         const int64_t b = min(row0 + 32 * (int64_t)(j + len), (hi + 31) & ~(int64_t)31);
-        if (a >= b) continue;
-        const uint32_t bytes = (uint32_t)(b - a) * (uint32_t)sizeof(T);
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(are + base + a), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(aim + base + a), "r"(bytes) : "memory");
+        if (a < b) f(a, b);
     }
+}
+__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+template <typename T>
+__device__ __forceinline__ void prefetch_tiles_l2(const T *are, const T *aim, int64_t base, int64_t lo, int64_t hi,
+                                                  uint32_t bits, int64_t row0) {
+    for_live_runs(bits, row0, lo, hi, [&](int64_t a, int64_t b) {
+        const uint32_t bytes = (uint32_t)(b - a) * (uint32_t)sizeof(T);
+        prefetch_l2(are + base + a, bytes);
+        prefetch_l2(aim + base + a, bytes);
+    });
 }
 
 // Mask bits of the `tiles` (1 .. 32) tiles from row row0 in the 1024-row mask word w.
