@@ -457,10 +457,18 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
             const uint32_t w = tmask ? tmask[(int64_t)(c0 + i) * mw + (row0 >> 10)] : 0xffffffffu;
             sq[i] = make_int4(m.off, (int)m.lo, (int)m.hi, (int)w);
             sb[i] = m.base;
-            // the block's tiles, inside one mask word
-            prefetch_tiles_l2(are, aim, m.base, m.lo, m.hi, block_tile_bits(w, row0, 8 / groups), row0);
         }
         __syncthreads();
+        {
+            // the block's tiles of diagonal i (inside one mask word), asked for after the barrier
+            // by lane i / 8 of warp i % 8, so that no warp waits on them
+            const int i = lane * 8 + wid;
+            if (i < cn) {
+                const int4 q = sq[i];
+                prefetch_tiles_l2(are, aim, sb[i], (int64_t)q.y, (int64_t)q.z,
+                                  block_tile_bits((uint32_t)q.w, row0, 8 / groups), row0);
+            }
+        }
         if (r >= rows) continue;
         il_accumulate32<G>(sq, sb, cn, r, g * (G / 4), quads, are, aim, xr, xi, accr, acci);
     }
