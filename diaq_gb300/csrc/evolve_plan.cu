@@ -395,12 +395,15 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // - When the block count is a multiple of 4, consecutive blocks take row blocks b, b + B/4,
 //   b + B/2, b + 3B/4 (B blocks): the blocks resident together spread over four distant parts of
 //   the rows (-2 %).
-// - While staging the metadata, the thread of each diagonal asks L2 for that diagonal's values in
-//   the block's live tiles (bulk prefetches, one per run of live tiles and plane), and thread 0
-//   for the block's own rows of the input states: the warps' matrix loads of the later diagonals
-//   then hit L2 (104.6 -> 100.1 us per 8-state term; 201 -> 178 us for 16 states).  Asking for
-//   the tiles of the block that launches one resident wave later instead made it slower (117 us),
-//   and so did asking, with each live run, for the state windows it reads (111 us).
+// - Right after the metadata barrier, lane i / 8 of warp i % 8 asks L2 for diagonal i's values in
+//   the block's live tiles (bulk prefetches, one per run of live tiles and plane), and thread 0,
+//   at block start, for the block's own rows of the input states: the warps' matrix loads of the
+//   later diagonals then hit L2 (104.6 -> 93.5 us per 8-state term, 201 -> 171 us for 16 states;
+//   issued by the staging threads before the barrier, where the other warps waited on them:
+//   100.1 us).  Asking for the tiles of the block that launches one resident wave later instead
+//   made it slower (117 us), and so did asking with each live run for the state windows it reads
+//   (111 us); asking at block start for the float64 states of the last step's epilogue changed
+//   nothing.
 template <class Epi, int G, int MINB>
 __global__ void __launch_bounds__(kSpmvThreads, MINB)
     dia_spmv_il32_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,

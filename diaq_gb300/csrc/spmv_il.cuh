@@ -210,7 +210,8 @@ __device__ __forceinline__ void il_accumulate32(const int4 *sq, const int64_t *s
                                                 const float *__restrict__ xr, const float *__restrict__ xi,
                                                 float (&accr)[G], float (&acci)[G]) {
     const int tbit = (r >> 5) & 31;
-#pragma unroll 4
+    // unrolled by 2: 93.1 us per 8-state Horner term on the 20-qubit chain (1 and 4: 95.0 and 93.9)
+#pragma unroll 2
     for (int k = 0; k < cn; ++k) {
         const int4 q = sq[k];
         if (r < q.y || r >= q.z || !(((uint32_t)q.w >> tbit) & 1u)) continue;
