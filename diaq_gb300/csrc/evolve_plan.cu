@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
             }
         }
         if (r >= rows) continue;
-        il_accumulate32<G>(sq, sb, cn, r, g * (G / 4), quads, are, aim, xr, xi, accr, acci);
+        il_accumulate32<G, true>(sq, sb, cn, r, g * (G / 4), quads, are, aim, xr, xi, accr, acci);
     }
     if constexpr (kTile) asm volatile("cp.async.wait_all;" ::: "memory");
     if (r >= rows) return;

@@ -174,19 +174,49 @@ __device__ __forceinline__ void il_load(int64_t c, int g0, int quads, const floa
         w.y[h] = __ldg(reinterpret_cast<const float4 *>(xi + at));
     }
 }
-// acc += (a + i b) * window, per state
-template <int G>
+// acc += (a + i b) * window, per state.  PACKED: two states per instruction (__ffma2_rn: each
+// lane one fmaf, the same rounding, so the same bits) -- 93.1 -> 91.1 us per 8-state Horner term
+// of the evolution plans; in the register-bounded batched kernels (six blocks per SM) it cost
+// 10 % (7,955 -> 7,122 states x steps/s), so they keep one FMA per state.
+template <int G, bool PACKED = false>
 __device__ __forceinline__ void il_fma(float a, float b, const IlWindow<G> &w, float (&accr)[G], float (&acci)[G]) {
+    if constexpr (PACKED) {
+        const float2 aa = make_float2(a, a), bb = make_float2(b, b), nb = make_float2(-b, -b);
 #pragma unroll
-    for (int h = 0; h < G / 4; ++h) {
-        const float xv[4] = {w.x[h].x, w.x[h].y, w.x[h].z, w.x[h].w};
-        const float yv[4] = {w.y[h].x, w.y[h].y, w.y[h].z, w.y[h].w};
+        for (int h = 0; h < G / 4; ++h) {
+            const float2 x01 = make_float2(w.x[h].x, w.x[h].y), x23 = make_float2(w.x[h].z, w.x[h].w);
+            const float2 y01 = make_float2(w.y[h].x, w.y[h].y), y23 = make_float2(w.y[h].z, w.y[h].w);
+            float2 r01 = make_float2(accr[4 * h], accr[4 * h + 1]), r23 = make_float2(accr[4 * h + 2], accr[4 * h + 3]);
+            float2 i01 = make_float2(acci[4 * h], acci[4 * h + 1]), i23 = make_float2(acci[4 * h + 2], acci[4 * h + 3]);
+            r01 = __ffma2_rn(aa, x01, r01);
+            r23 = __ffma2_rn(aa, x23, r23);
+            r01 = __ffma2_rn(nb, y01, r01);
+            r23 = __ffma2_rn(nb, y23, r23);
+            i01 = __ffma2_rn(aa, y01, i01);
+            i23 = __ffma2_rn(aa, y23, i23);
+            i01 = __ffma2_rn(bb, x01, i01);
+            i23 = __ffma2_rn(bb, x23, i23);
+            accr[4 * h] = r01.x;
+            accr[4 * h + 1] = r01.y;
+            accr[4 * h + 2] = r23.x;
+            accr[4 * h + 3] = r23.y;
+            acci[4 * h] = i01.x;
+            acci[4 * h + 1] = i01.y;
+            acci[4 * h + 2] = i23.x;
+            acci[4 * h + 3] = i23.y;
+        }
+    } else {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            accr[4 * h + q] = fmaf(a, xv[q], accr[4 * h + q]);
-            accr[4 * h + q] = fmaf(-b, yv[q], accr[4 * h + q]);
-            acci[4 * h + q] = fmaf(a, yv[q], acci[4 * h + q]);
-            acci[4 * h + q] = fmaf(b, xv[q], acci[4 * h + q]);
+        for (int h = 0; h < G / 4; ++h) {
+            const float xv[4] = {w.x[h].x, w.x[h].y, w.x[h].z, w.x[h].w};
+            const float yv[4] = {w.y[h].x, w.y[h].y, w.y[h].z, w.y[h].w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                accr[4 * h + q] = fmaf(a, xv[q], accr[4 * h + q]);
+                accr[4 * h + q] = fmaf(-b, yv[q], accr[4 * h + q]);
+                acci[4 * h + q] = fmaf(a, yv[q], acci[4 * h + q]);
+                acci[4 * h + q] = fmaf(b, xv[q], acci[4 * h + q]);
+            }
         }
     }
 }
@@ -204,7 +234,7 @@ __device__ __forceinline__ void il_term(int64_t c, int g0, int quads, float a, f
 // and n_pad * sp below 2^31).  sq[k] = (offset, lo, hi, mask word of the block's rows), sb[k] =
 // value base: one 16-byte and one 8-byte shared-memory load per diagonal; a warp skips a dead
 // tile or a diagonal outside its rows together.
-template <int G>
+template <int G, bool PACKED = false>
 __device__ __forceinline__ void il_accumulate32(const int4 *sq, const int64_t *sb, int cn, int r, int g0, int quads,
                                                 const float *__restrict__ are, const float *__restrict__ aim,
                                                 const float *__restrict__ xr, const float *__restrict__ xi,
@@ -225,7 +255,7 @@ __device__ __forceinline__ void il_accumulate32(const int4 *sq, const int64_t *s
             w.x[h] = __ldg(reinterpret_cast<const float4 *>(xr + at));
             w.y[h] = __ldg(reinterpret_cast<const float4 *>(xi + at));
         }
-        il_fma<G>(a, b, w, accr, acci);
+        il_fma<G, PACKED>(a, b, w, accr, acci);
     }
 }
 

@@ -413,3 +413,42 @@ def test_horner_il32_ragged_sizes(native, N, k):
     for q in (0, k - 1):
         want = orc.ham_sim(A, P[q], 0.06, 3, 12)
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, q
+
+
+@pytest.mark.parametrize("mode", ["horner", "mixed"])
+@pytest.mark.parametrize("N,k", [(1500, 8), (2048 + 96, 8), (777, 16), (3000, 4)])
+def test_il32_same_bits_as_variant_9(native, mode, N, k):
+    """Variant 12 (32-bit loop, L2 prefetches, block swizzle, fp32(psi) tile, packed two-lane
+    FMAs, middle and last terms as separate instantiations) does the sums of variant 9 in the same
+    order with the same roundings: the evolved states agree bit for bit."""
+    import torch
+
+    capi, _ = native
+    rng = np.random.default_rng(N + k)
+    offs = sorted({0, 1, 2, 33, 64, 100, N // 3, N - 7})
+    off, re, im = [], [], []
+    for d in offs:
+        L = N - d
+        a = rng.standard_normal(L) + 1j * rng.standard_normal(L)
+        if d == 0:
+            a = a.real + 0j
+        a[rng.random(L) < 0.5] = 0
+        for dd, v in ((d, a), (-d, np.conj(a))) if d else ((0, a),):
+            off.append(dd)
+            re.append(v.real * 0.3)
+            im.append(v.imag * 0.3)
+    order = np.argsort(off)
+    off = np.asarray(off, dtype=np.int32)[order]
+    re = np.concatenate([re[i] for i in order])
+    im = np.concatenate([im[i] for i in order])
+    H = capi.Matrix.create(N, N, off, re, im)
+    P = ham.random_state(N, 5, k=k)
+    out = []
+    for variant in (9, 12):
+        E = capi.Evolve(H, k, capi.EVOLVE_HORNER if mode == "horner" else capi.EVOLVE_MIXED)
+        E.set_config(4, 1, variant)
+        pr = torch.from_numpy(np.ascontiguousarray(P.real)).cuda()
+        pi = torch.from_numpy(np.ascontiguousarray(P.imag)).cuda()
+        E.run(pr, pi, N, 0.03, 4, 0, 11)
+        out.append(_result(pr, pi))
+    assert np.array_equal(out[0], out[1])
