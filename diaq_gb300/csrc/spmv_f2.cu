@@ -7,9 +7,9 @@
 // kernel accumulates products of such pairs exactly enough on the FP32 pipes:
 //   product   p = ah*xh (+ error fma(ah, xh, -p)) + ah*xl + al*xh          (Dekker/Knuth with FMA)
 //   sum       (sh, sl) <- TwoSum(sh, p) with the error and the low parts added to sl
-// About 12 FP32 instructions per real product-accumulate, 48 per complex value: ~0.7 T complex
-// values/s, above the ~0.42 T/s at which HBM delivers the 16-byte values -- the kernel becomes
-// memory-bound.  Relative error ~1e-14 (2^-48 per value plus accumulation): inside the 1e-12 of
+// About 12 FP32 operations per real product-accumulate, 48 per complex value, issued as packed
+// two-lane instructions over pairs of rows (24 per complex value and row): ~0.7 T complex values/s
+// or more, above the ~0.42 T/s at which HBM delivers the 16-byte values.  Relative error ~1e-14 (2^-48 per value plus accumulation): inside the 1e-12 of
 // the float64 path's parity bar.  Range: magnitudes in roughly [1e-30, 1e38] keep the full
 // precision (the low float must stay normal).
 //
@@ -116,23 +116,26 @@ __global__ void f2_split_pair_kernel(const double *__restrict__ xr, const double
     }
 }
 
-struct F2 {
-    float h, l;
+// s += a*x for float pairs (see the file comment), two rows at once: TwoProd (ph + the exact
+// remainder by FMA) and TwoSum, on the packed two-lane FP32 instructions (__fmul2_rn, __ffma2_rn,
+// __fadd2_rn: each lane the scalar operation with its rounding; a - b as a + (-b), which is exact).
+// The _rn intrinsics keep the compiler from fusing the product into the sum, which would break
+// both identities.  Negate ah and al to subtract.  Against one row per instruction: 101.1 -> 99.5
+// us per SpMV on the 20-qubit chain, the same bits.
+struct F2P {
+    float2 h, l;
 };
-
-// s += a*x for float pairs (see the file comment); sign = -1 subtracts.
-__device__ __forceinline__ void f2_mac(F2 &s, float ah, float al, float xh, float xl, float sign) {
-    // TwoProd (ph + exact remainder via fma) and TwoSum; the _rn intrinsics keep the compiler from
-    // fusing the product into the sum, which would break both identities
-    const float ph = __fmul_rn(sign * ah, xh);
-    float pl = fmaf(sign * ah, xh, -ph);
-    pl = fmaf(sign * ah, xl, pl);
-    pl = fmaf(sign * al, xh, pl);
-    const float t = __fadd_rn(s.h, ph);
-    const float bb = __fsub_rn(t, s.h);
-    const float e = __fadd_rn(__fsub_rn(s.h, __fsub_rn(t, bb)), __fsub_rn(ph, bb));
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+__device__ __forceinline__ void f2_mac2(F2P &s, float2 ah, float2 al, float2 xh, float2 xl) {
+    const float2 ph = __fmul2_rn(ah, xh);
+    float2 pl = __ffma2_rn(ah, xh, neg2(ph));
+    pl = __ffma2_rn(ah, xl, pl);
+    pl = __ffma2_rn(al, xh, pl);
+    const float2 t = __fadd2_rn(s.h, ph);
+    const float2 bb = __fadd2_rn(t, neg2(s.h));
+    const float2 e = __fadd2_rn(__fadd2_rn(s.h, neg2(__fadd2_rn(t, neg2(bb)))), __fadd2_rn(ph, neg2(bb)));
     s.h = t;
-    s.l += e + pl;
+    s.l = __fadd2_rn(s.l, __fadd2_rn(e, pl));
 }
 
 // y = A x: each thread owns VR = 4 consecutive rows; hi and lo planes are separate SoA arrays, so
@@ -156,9 +159,9 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
     const int lane = threadIdx.x & 31;
     const int64_t r0 = ((int64_t)blockIdx.x * kSpmvThreads + threadIdx.x) * V;
     const int64_t w0 = r0 - (int64_t)V * lane;
-    F2 sr[V], si[V];
+    F2P sr[V / 2], si[V / 2];   // rows (0, 1) and (2, 3)
 #pragma unroll
-    for (int v = 0; v < V; ++v) sr[v] = si[v] = F2{0.f, 0.f};
+    for (int v = 0; v < V / 2; ++v) sr[v] = si[v] = F2P{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
     for (int c0 = 0; c0 < nd; c0 += kMetaChunk) {
         const int cn = min(kMetaChunk, nd - c0);
         __syncthreads();
@@ -210,11 +213,15 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
                 }
             }
 #pragma unroll
-            for (int v = 0; v < V; ++v) {
-                f2_mac(sr[v], arh[v], arl[v], xrhv[v], xrlv[v], 1.f);
-                f2_mac(sr[v], aih[v], ail[v], xihv[v], xilv[v], -1.f);
-                f2_mac(si[v], arh[v], arl[v], xihv[v], xilv[v], 1.f);
-                f2_mac(si[v], aih[v], ail[v], xrhv[v], xrlv[v], 1.f);
+            for (int v = 0; v < V; v += 2) {
+                const float2 rh = make_float2(arh[v], arh[v + 1]), rl = make_float2(arl[v], arl[v + 1]);
+                const float2 ih = make_float2(aih[v], aih[v + 1]), il = make_float2(ail[v], ail[v + 1]);
+                const float2 xrh2 = make_float2(xrhv[v], xrhv[v + 1]), xrl2 = make_float2(xrlv[v], xrlv[v + 1]);
+                const float2 xih2 = make_float2(xihv[v], xihv[v + 1]), xil2 = make_float2(xilv[v], xilv[v + 1]);
+                f2_mac2(sr[v / 2], rh, rl, xrh2, xrl2);
+                f2_mac2(sr[v / 2], neg2(ih), neg2(il), xih2, xil2);
+                f2_mac2(si[v / 2], rh, rl, xih2, xil2);
+                f2_mac2(si[v / 2], ih, il, xrh2, xrl2);
             }
         }
     }
@@ -222,8 +229,9 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
 #pragma unroll
     for (int v = 0; v < V; ++v)
         if (r0 + v < rows) {
-            yr[r0 + v] = (double)sr[v].h + (double)sr[v].l;
-            yi[r0 + v] = (double)si[v].h + (double)si[v].l;
+            const F2P &a = sr[v / 2], &b = si[v / 2];
+            yr[r0 + v] = (double)((v & 1) ? a.h.y : a.h.x) + (double)((v & 1) ? a.l.y : a.l.x);
+            yi[r0 + v] = (double)((v & 1) ? b.h.y : b.h.x) + (double)((v & 1) ? b.l.y : b.l.x);
         }
 }
 
