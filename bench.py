@@ -37,7 +37,7 @@ METRIC = "expm(-iHt)·ψ states·steps/s"
 # variant): for variant 12 the mean over the 12 launches of one time step (first, middle and last
 # terms, as roofline.achieved averages them); for variant 9 one middle term.  The kernels skip
 # all-zero 32-row tiles.
-TRAFFIC_PER_LAUNCH = {(20, 8, "horner", 4, 1, 9): 390.6e6, (20, 8, "horner", 4, 1, 12): 378.4e6}
+TRAFFIC_PER_LAUNCH = {(20, 8, "horner", 4, 1, 9): 390.6e6, (20, 8, "horner", 4, 1, 12): 378.3e6}
 
 
 def peaks():
