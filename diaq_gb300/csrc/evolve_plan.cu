@@ -494,7 +494,8 @@ __global__ void __launch_bounds__(kSpmvThreads, MINB)
 // ---- the plan ------------------------------------------------------------------------------------------
 struct EvolvePlan {
     const Matrix *H = nullptr;   // the caller's matrix (c128)
-    Matrix *Hc = nullptr;        // owned c64 copy (MIXED)
+    Matrix *Hc = nullptr;        // c64 copy (float32-term modes)
+    bool owns_hc = true;         // Hc and tmask are this plan's own (else borrowed from the plan that owns this one)
     int mode = 0, nrhs = 1;
     int64_t n = 0;
     void *buf = nullptr;         // work vectors
@@ -526,6 +527,12 @@ struct EvolvePlan {
     int sp = 4;           // interleaved layout: nrhs rounded up to a power of two >= 4 (<= 32 used)
     int64_t n_pad = 0;    // rows rounded up to a multiple of 32
     double *stage = nullptr;  // device copy of the states for diaq_evolve_run_host, 2 * nrhs * n
+    // diaq_evolve_run_host, one step of an even number (>= 8) of float32-term states: two plans
+    // for the two halves of the states, run one after the other on stream hcomp while the second
+    // half is copied up and the first copied down (events hsev)
+    EvolvePlan *half[2] = {nullptr, nullptr};
+    cudaStream_t hcomp = nullptr;
+    cudaEvent_t hsev[4] = {nullptr, nullptr, nullptr, nullptr};
 
     bool f32() const { return mode == DIAQ_EVOLVE_MIXED || mode == DIAQ_EVOLVE_HORNER; }
     bool interleaved() const { return f32() && cfg.pipe >= 6; }
@@ -536,17 +543,21 @@ struct EvolvePlan {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
         if (buf) cudaFree(buf);
         if (part) cudaFree(part);
-        if (tmask) cudaFree(tmask);
+        if (tmask && owns_hc) cudaFree(tmask);
         if (err) cudaFree(err);
         if (err_host) cudaFreeHost(err_host);
         if (err_ev) cudaEventDestroy(err_ev);
         if (stage) cudaFree(stage);
-        if (Hc) destroy(Hc);
+        if (Hc && owns_hc) destroy(Hc);
         if (s) cudaStreamDestroy(s);
         for (int j = 0; j < 2; ++j) {
             if (hs[j]) cudaStreamDestroy(hs[j]);
             if (hev[j]) cudaEventDestroy(hev[j]);
+            delete half[j];
         }
+        if (hcomp) cudaStreamDestroy(hcomp);
+        for (auto ev : hsev)
+            if (ev) cudaEventDestroy(ev);
     }
 };
 
@@ -639,7 +650,9 @@ static int allow_tma_smem() {
     return DIAQ_OK;
 }
 
-static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
+// share: a float32-term plan of the same matrix whose c64 copy and zero-tile mask the new plan
+// borrows instead of making its own (the half plans of diaq_evolve_run_host); NULL: its own.
+static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out, const EvolvePlan *share = nullptr) {
     if (H.rows != H.cols) return set_error(DIAQ_ERR_INVALID, "evolve: H must be square");
     if (H.prec != DIAQ_C128) return set_error(DIAQ_ERR_INVALID, "evolve: pass the c128 matrix (the plan makes its own c64 copy)");
     if (nrhs < 1) return set_error(DIAQ_ERR_INVALID, "evolve: nrhs must be >= 1");
@@ -662,7 +675,13 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
                                                                          vec) * sizeof(float);
     if (e == cudaSuccess && bytes) e = dev_malloc(&P->buf, bytes);
     if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
-    if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
+    const bool borrow = share && share->Hc && mode != DIAQ_EVOLVE_C128;
+    if (borrow) {
+        P->Hc = share->Hc;
+        P->tmask = share->tmask;
+        P->owns_hc = false;
+    }
+    if (st == DIAQ_OK && mode != DIAQ_EVOLVE_C128 && !borrow) st = copy_as(H, DIAQ_C64, P->s, &P->Hc);
     if (st == DIAQ_OK && mode == DIAQ_EVOLVE_MIXED) st = allow_tma_smem<EpiMixedIL>();
     if (st == DIAQ_OK && mode == DIAQ_EVOLVE_HORNER) st = allow_tma_smem<EpiHornerT<0>>();
     if (st == DIAQ_OK && mode == DIAQ_EVOLVE_HORNER) st = allow_tma_smem<EpiHornerT<1>>();
@@ -674,7 +693,7 @@ static int plan_create(const Matrix &H, int nrhs, int mode, EvolvePlan **out) {
         if (e == cudaSuccess) *P->err_host = 0;
         if (e != cudaSuccess) st = cuda_status(e, "evolve plan", __FILE__, __LINE__);
     }
-    if (st == DIAQ_OK && H.nd > 0) {
+    if (st == DIAQ_OK && H.nd > 0 && !borrow) {
         // the mask of the plan's own c64 copy is built once; that of the caller's c128 matrix
         // again at every run (its values may have changed)
         e = dev_malloc(&P->tmask, sizeof(uint32_t) * (size_t)H.nd * (size_t)tile_mask_words(H.rows));
@@ -1206,6 +1225,82 @@ int diaq_evolve_config(diaq_evolve_t E, int *states_per_block, int *rows_per_thr
     return DIAQ_OK;
 }
 
+}  // extern "C"
+
+namespace diaq_gb300 {
+
+// One step of the states in host memory as two half plans, so that the link and the GPU work at
+// once: half 0 up; half 0 runs while half 1 goes up; half 1 runs while half 0 comes down; half 1
+// down.  The states of a half are contiguous in each plane (state q at psi[q n + r]).  Each half
+// plan runs the launch shape of the whole plan (the same sums per state, so the same bits as
+// an unsplit run) with the whole plan's settings.
+static int run_host_split(EvolvePlan &E, double *psi_re, double *psi_im, double dt, int sl, int m) {
+    const int h = E.nrhs / 2;
+    const size_t cnt = (size_t)E.nrhs * (size_t)E.n, hc = (size_t)h * (size_t)E.n;
+    for (int j = 0; j < 2; ++j) {
+        if (!E.half[j]) {
+            DQ_TRY(plan_create(*E.H, h, E.mode, &E.half[j], &E));
+            E.half[j]->cfg = E.cfg;
+            E.half[j]->tuned = true;
+        }
+        EvolvePlan &Hp = *E.half[j];
+        if (Hp.wait_ns != E.wait_ns || Hp.renorm != E.renorm || Hp.cfg.kmax != E.cfg.kmax || Hp.cfg.vr != E.cfg.vr ||
+            Hp.cfg.pipe != E.cfg.pipe) {
+            Hp.wait_ns = E.wait_ns;
+            Hp.renorm = E.renorm;
+            Hp.cfg = E.cfg;
+            for (auto &kv : Hp.graphs) cudaGraphExecDestroy(kv.second);
+            Hp.graphs.clear();
+        }
+    }
+    if (!E.hcomp) DQ_CUDA(cudaStreamCreateWithFlags(&E.hcomp, cudaStreamNonBlocking));
+    for (auto &ev : E.hsev)
+        if (!ev) DQ_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    double *d = E.stage;
+    cudaStream_t up = E.hs[0], down = E.hs[1], comp = E.hcomp;
+    const size_t hb = hc * sizeof(double);
+    cudaError_t e = cudaSuccess;
+    int st = DIAQ_OK;
+    // up: both halves on one stream, an event after each
+    for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+        e = cudaMemcpyAsync(d + j * hc, psi_re + j * hc, hb, cudaMemcpyHostToDevice, up);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + cnt + j * hc, psi_im + j * hc, hb, cudaMemcpyHostToDevice, up);
+        if (e == cudaSuccess) e = cudaEventRecord(E.hsev[j], up);
+    }
+    if (e != cudaSuccess) st = cuda_status(e, "evolve upload", __FILE__, __LINE__);
+    // run: each half once its states have landed, one after the other on comp
+    for (int j = 0; j < 2 && st == DIAQ_OK; ++j) {
+        e = cudaStreamWaitEvent(comp, E.hsev[j], 0);
+        if (e != cudaSuccess) {
+            st = cuda_status(e, "evolve run_host", __FILE__, __LINE__);
+            break;
+        }
+        st = plan_run(*E.half[j], d + j * hc, d + cnt + j * hc, E.n, dt, 1, sl, m, comp);
+        if (st == DIAQ_OK) {
+            e = cudaEventRecord(E.hsev[2 + j], comp);
+            if (e != cudaSuccess) st = cuda_status(e, "evolve run_host", __FILE__, __LINE__);
+        }
+    }
+    // down: each half once it has run
+    for (int j = 0; j < 2 && st == DIAQ_OK; ++j) {
+        e = cudaStreamWaitEvent(down, E.hsev[2 + j], 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(psi_re + j * hc, d + j * hc, hb, cudaMemcpyDeviceToHost, down);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(psi_im + j * hc, d + cnt + j * hc, hb, cudaMemcpyDeviceToHost, down);
+        if (e != cudaSuccess) st = cuda_status(e, "evolve download", __FILE__, __LINE__);
+    }
+    const cudaError_t eu = cudaStreamSynchronize(up), ec = cudaStreamSynchronize(comp),
+                      ed = cudaStreamSynchronize(down);
+    if (st == DIAQ_OK && eu != cudaSuccess) st = cuda_status(eu, "evolve run_host", __FILE__, __LINE__);
+    if (st == DIAQ_OK && ec != cudaSuccess) st = cuda_status(ec, "evolve run_host", __FILE__, __LINE__);
+    if (st == DIAQ_OK && ed != cudaSuccess) st = cuda_status(ed, "evolve run_host", __FILE__, __LINE__);
+    for (int j = 0; j < 2 && st == DIAQ_OK; ++j) st = take_wait_error(*E.half[j], true);
+    return st;
+}
+
+}  // namespace diaq_gb300
+
+extern "C" {
+
 int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
                          int substeps_log2, int m) {
     if (!E) return set_error(DIAQ_ERR_INVALID, "evolve plan is NULL");
@@ -1219,6 +1314,12 @@ int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double
         if (!E->hs[j]) DQ_CUDA(cudaStreamCreateWithFlags(&E->hs[j], cudaStreamNonBlocking));
         if (!E->hev[j]) DQ_CUDA(cudaEventCreateWithFlags(&E->hev[j], cudaEventDisableTiming));
     }
+    // a single step of 8 or more float32-term states, once the plan has its launch shape: the
+    // halves overlap the copies with the run (on the 20-qubit chain, 8 states: the copies take
+    // ~1.4 ms per step against 1.1 ms of run)
+    if (steps == 1 && m > 0 && E->f32() && E->tuned && E->nrhs >= 8 && E->nrhs % 2 == 0 && std::isfinite(dt) &&
+        substeps_log2 >= 0 && substeps_log2 <= 20)
+        return run_host_split(*E, psi_re, psi_im, dt, substeps_log2, m);
     double *d = E->stage;
     cudaStream_t a = E->hs[0], b = E->hs[1];
     const size_t bytes = cnt * sizeof(double);

@@ -270,7 +270,11 @@ int diaq_evolve_run(diaq_evolve_t E, double *psi_re, double *psi_im, int64_t ld,
 /* diaq_evolve_run with host arrays: the nrhs states (state q at psi[q*N ..]) are copied to the
  * device, advanced, and copied back.  Synchronous.  The device copy of the states belongs to the
  * plan: allocated by the first call, reused by the later ones, freed with the plan.
- * A wait that gave up during the run is reported by this call (DIAQ_ERR_TIMEOUT). */
+ * A wait that gave up during the run is reported by this call (DIAQ_ERR_TIMEOUT).
+ * One step (steps == 1) of an even nrhs >= 8 in the float32-term modes, once the plan has its
+ * launch shape, runs as two plans of nrhs / 2 states (made on first use, sharing the plan's
+ * float32 matrix): the second half is copied up and the first copied down while the GPU works;
+ * the results are the same bits. */
 int diaq_evolve_run_host(diaq_evolve_t E, double *psi_re, double *psi_im, double dt, int64_t steps,
                          int substeps_log2, int m);
 

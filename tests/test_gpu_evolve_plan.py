@@ -129,6 +129,43 @@ def test_run_host_calls_in_a_row(native, mode):
         assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < tol, q
 
 
+@pytest.mark.parametrize("mode,k,renorm", [("horner", 8, False), ("mixed", 8, True), ("horner", 10, True),
+                                           ("horner", 16, False)])
+def test_run_host_single_steps_split_same_bits(native, mode, k, renorm):
+    """One step per diaq_evolve_run_host call of 8 or more float32-term states runs as two half
+    plans overlapping the copies with the run: the same bits as the same steps on device buffers
+    through diaq_evolve_run (one step per call), and within the 1e-6 bar of the oracle."""
+    import torch
+
+    capi, _ = native
+    N, off, re, im = ham.xxz(12)
+    A = orc.OMatrix(N, N, off, re, im)
+    H = capi.Matrix.create(N, N, off, re, im)
+    md = capi.EVOLVE_HORNER if mode == "horner" else capi.EVOLVE_MIXED
+    P = ham.random_state(N, 1, k=k)
+    Eh, Ed = capi.Evolve(H, k, md), capi.Evolve(H, k, md)
+    for E in (Eh, Ed):
+        E.set_config(4, 1, 12)
+        E.set_renormalize(renorm)
+    hr = np.ascontiguousarray(P.real).ravel().copy()
+    hi = np.ascontiguousarray(P.imag).ravel().copy()
+    pr = torch.from_numpy(np.ascontiguousarray(P.real)).cuda()
+    pi = torch.from_numpy(np.ascontiguousarray(P.imag)).cuda()
+    for i in range(3):
+        dt = 0.04 + 0.01 * i
+        Eh.run_host(hr, hi, dt, 1, 0, 11)
+        Ed.run(pr, pi, N, dt, 1, 0, 11)
+    got = (hr + 1j * hi).reshape(k, N)
+    assert np.array_equal(got, _result(pr, pi))
+    for q in (0, k // 2, k - 1):
+        want = P[q]
+        for i in range(3):
+            want = orc.ham_sim(A, want, 0.04 + 0.01 * i, 1, 11)
+            if renorm:
+                want = want / np.linalg.norm(want)
+        assert np.linalg.norm(got[q] - want) / np.linalg.norm(want) < 1e-6, q
+
+
 def test_plan_rejects_bad_input(native):
     capi, _ = native
     M = capi.Matrix.create(4, 6, [0], np.ones(4), np.zeros(4))
