@@ -66,3 +66,15 @@ def test_live_macs_against_brute_force():
                 if 0 <= r + da < N and rl[da][r] and rl[db][r + da]:
                     want += 1
     assert bench._live_macs(N, off, re, im) == want
+
+
+def test_cpu_baseline_sample_returns_the_evolved_state():
+    """The CPU baseline sample evolves psi0 (seed 0) for the steps it reports and returns that
+    state: the reference the bench line's state-0 accuracy is measured against."""
+    from oracle import oracle as orc
+
+    N, off, re, im = ham.xxz(8)
+    base, psi, done = bench.cpu_baseline_sample(N, off, re, im, 1, 6, steps=3)
+    assert done == 3 and base["unit"] == "states·steps/s" and base["value"] > 0 and base["kind"] == "port"
+    want = orc.ham_sim(orc.OMatrix(N, N, off, re, im), ham.random_state(N, 0), 3 * bench.DT, 3, 6, substeps=2)
+    assert np.linalg.norm(psi - want) / np.linalg.norm(want) < 1e-12
