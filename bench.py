@@ -1165,7 +1165,8 @@ def run_ours(args, rank, world):
         "e2e": {"value": world * S * K / e2e_s, "unit": "states·steps/s", "h2d_bytes_per_step": 16 * N * S,
                 "d2h_bytes_per_step": 16 * N * S, "host_memory": host_mem,
                 "note": "K calls of diaq_evolve_run_host, each: S float64 states host to device, one time step, "
-                        "S states device to host"},
+                        "S states device to host (the library runs the two halves of the states one after the "
+                        "other, each half's copies overlapping the other's run)"},
         "e2e_one_call": {"value": world * S * K / e2e_one_s, "unit": "states·steps/s",
                          "h2d_bytes_per_step": 16 * N * S / K, "d2h_bytes_per_step": 16 * N * S / K,
                          "note": "one diaq_evolve_run_host call: S states up, K steps, S states down"},
