@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // in one 16-byte shared-memory record, the value base in a second array: fewer registers and one
 // shared-memory load per diagonal.
 //
-// Two more measures, both bit-neutral:
+// Further measures, all bit-neutral:
 // - An epilogue that reads an fp32(psi) quad per plane and row (the Horner middle step,
 //   Epi::kPsiTile) gets it from shared memory: each lane copies its quads with cp.async when the
 //   warp starts and waits for them only after its diagonal loop, so the epilogue no longer stalls
@@ -404,6 +404,10 @@ __global__ void __launch_bounds__(kSpmvThreads)
 //   made it slower (117 us), and so did asking with each live run for the state windows it reads
 //   (111 us); asking at block start for the float64 states of the last step's epilogue changed
 //   nothing.
+// - The multiply-adds run two states per instruction (il_fma's packed form, __ffma2_rn): 58.0 M
+//   instead of 67.5 M instructions per launch, 93.1 -> 91.1 us per 8-state term.
+// - The Horner epilogue's middle and last steps are separate instantiations (EpiHornerT<0> and
+//   <1>): the middle steps' kernel holds no float64 code.
 template <class Epi, int G, int MINB>
 __global__ void __launch_bounds__(kSpmvThreads, MINB)
     dia_spmv_il32_kernel(const DiagMeta *__restrict__ meta, int nd, const float *__restrict__ are,
